@@ -1,0 +1,90 @@
+"""Seeded synthetic workloads with the shapes and distributions of the five
+benchmark configurations (orbital elements; angles in radians).
+
+The reference ships no particle state for its examples (the 200,000-particle
+resonance state is not distributed), so every workload here is generated:
+numpy's default generator seeded per configuration draws the elements and
+`from_elements_M` (src/convert.cpp:257-275, restated in the library) turns
+them into heliocentric Cartesian states.
+"""
+import numpy as np
+
+DEG = np.pi / 180.0
+GM_SUN_AU_DAY = 2.959122e-4            # G*Msun in au^3/day^2 (G = 1 units)
+GM_SUN_AU_YR = 4 * np.pi ** 2          # G*Msun in au^3/yr^2
+
+GIANT_MASSES = np.array([9.55e-4, 2.86e-4, 4.37e-5, 5.15e-5])   # in Msun
+GIANT_A = np.array([5.2, 9.55, 19.2, 30.1])
+NEPTUNE_MASS = 5.15e-5
+
+
+def _angles(rng, n):
+    return rng.uniform(0, 2 * np.pi, n), rng.uniform(0, 2 * np.pi, n), rng.uniform(0, 2 * np.pi, n)
+
+
+def particle_elements(rng, n, a_range, e_range, i_max_deg, log_a=False):
+    """Elements [n, 6] = a, e, i, capom, om, M with uniform angles."""
+    if log_a:
+        a = np.exp(rng.uniform(np.log(a_range[0]), np.log(a_range[1]), n))
+    else:
+        a = rng.uniform(a_range[0], a_range[1], n)
+    e = rng.uniform(e_range[0], e_range[1], n)
+    inc = rng.uniform(0, i_max_deg * DEG, n)
+    O, o, M = _angles(rng, n)
+    return np.stack([a, e, inc, O, o, M], axis=1)
+
+
+def neptune_planets(gm_sun=GM_SUN_AU_DAY, a=30.0):
+    """Sun + one Neptune-mass planet on a circular, planar orbit (configs 1, 3, 5).
+    Returns (masses [2], elements [1, 6])."""
+    m = np.array([gm_sun, NEPTUNE_MASS * gm_sun])
+    el = np.array([[a, 0.0, 0.0, 0.0, 0.0, 0.0]])
+    return m, el
+
+
+def giant_planets(rng, gm_sun=GM_SUN_AU_DAY, mass_scale=None, a_scale=None):
+    """Sun + four giants with e~U(0,0.05), i~U(0,2 deg) (configs 2, 4)."""
+    ms = GIANT_MASSES * (mass_scale if mass_scale is not None else 1.0)
+    a = GIANT_A * (a_scale if a_scale is not None else 1.0)
+    e = rng.uniform(0, 0.05, 4)
+    inc = rng.uniform(0, 2 * DEG, 4)
+    O, o, M = _angles(rng, 4)
+    m = np.concatenate([[gm_sun], ms * gm_sun])
+    return m, np.stack([a, e, inc, O, o, M], axis=1)
+
+
+CONFIGS = {
+    1: dict(name="plain-neptune", n=2000, dt=180.0, steps=10000, tbsize=128, cull=0.5, outer=300.0,
+            planets="neptune", a=(40, 50), e=(0, 0.1), i=5.0),
+    2: dict(name="plain-giants", n=1_000_000, dt=180.0, steps=200_000, tbsize=2048, cull=0.5, outer=300.0,
+            planets="giants", a=(53, 57), e=(0, 0.3), i=10.0),
+    3: dict(name="scattered-disk", n=1_000_000, dt=180.0, steps=50_000, tbsize=512, cull=0.5, outer=1e5,
+            planets="neptune", a=(30, 1000), e=(0, 0.95), i=40.0, log_a=True),
+    4: dict(name="ensembles", systems=256, median=20000, clip=(1000, 200000), dt=180.0, steps=10000, tbsize=1024,
+            cull=0.5, outer=300.0, planets="giants", a=(40, 50), e=(0, 0.1), i=5.0),
+    5: dict(name="history-encounters", n=2_000_000, dt=0.2, steps=50_000, tbsize=100, cull=0.5, outer=300.0,
+            planets="neptune-yr", a=(20, 40), e=(0, 0.3), i=10.0, esf=3.0, hist_every=100),
+}
+
+
+def workload(cfg_id, n=None, seed=0):
+    """Returns dict(pl_m [npl], pl_el [npl-1, 6], el [n, 6], **cfg) for a config."""
+    c = dict(CONFIGS[cfg_id])
+    rng = np.random.default_rng(seed)
+    if c["planets"] == "neptune":
+        m, pel = neptune_planets()
+    elif c["planets"] == "neptune-yr":
+        m, pel = neptune_planets(GM_SUN_AU_YR)
+    else:
+        m, pel = giant_planets(rng)
+    n = c.get("n", 0) if n is None else n
+    el = particle_elements(rng, n, c["a"], c["e"], c["i"], c.get("log_a", False))
+    c.update(pl_m=m, pl_el=pel, el=el, n=n)
+    return c
+
+
+def ensemble_counts(systems=256, median=20000, clip=(1000, 200000), sigma=1.0, seed=0):
+    """Lognormal particle counts per system (config 4)."""
+    rng = np.random.default_rng(seed)
+    c = np.exp(rng.normal(np.log(median), sigma, systems))
+    return np.clip(np.round(c), clip[0], clip[1]).astype(np.int64)
