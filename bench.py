@@ -1,0 +1,347 @@
+"""Benchmark: particle-steps/s of the massless-particle WH/MVS time-block
+integrator on GB300.
+
+Workload (default): Sun + four giant planets, 1,000,000 particles near the
+Neptune 3:1 (a~U(53,57) au, e~U(0,0.3), i~U(0,10 deg)), FP64, dt = 180 d,
+Time-Block-Size 2048.  One bench step = one time block (2048 steps of every
+alive particle), so a step is ~2e9 particle-steps.  The particle state is
+generated from seeded synthetic elements (the reference ships no state for
+this configuration).
+
+Outputs one JSON line (rank 0).  `value` is device-resident throughput over
+K blocks timed with CUDA events on the executor's stream; `e2e` repeats the
+blocks through the C ABI with host buffers (state uploaded and downloaded
+every block inside the timed region).  `roofline` relates the time-block
+kernel's algorithmic FP64 flops (F = 99 + 14*5 + 18*Np per particle-step) to
+the FP64 FMA throughput the library's probe measures on the same GPU.
+`cpu_baseline` times the oracle's restatement of the reference kernel on the
+host cores.  `--impl reference` times that CPU implementation as the arm.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s on 1 GB300, learned+batched vs plain, at <=1e-10 rel pos err"
+UNIT = "particle-steps/s"
+
+
+def alg_flops_per_particle_step(n_planets, k_ref=5):
+    """Algorithmic FP64 flops per particle-step (reference formulation):
+    2 kicks 12, drift prelude 45, K Newton passes 14 each, f/g and the new
+    state 37, 18 per planet, 5 for the Sun/outer tests."""
+    return 99 + 14 * k_ref + 18 * n_planets
+
+
+def config_text(tbsize, dt, outer=300.0):
+    return ("Time-Step %r\nTime-Block-Size %d\nFinal-Time 1e30\nOuter-Limit %r\nCull-Radius 0.5\n"
+            "Input-File unused\nOutput-Folder unused\n" % (dt, tbsize, outer))
+
+
+def make_state(G, n, cfg_id, rank):
+    from glisser_gb300 import synth
+    w = synth.workload(cfg_id, n=0, seed=0)          # planets: seed 0 on every rank
+    el = synth.workload(cfg_id, n=n, seed=1000 + rank)["el"]
+    m = w["pl_m"]
+    pr, pv = [np.zeros(3)], [np.zeros(3)]
+    for k in range(len(m) - 1):
+        a, b = G.elements_to_cartesian(m[0] + m[k + 1], w["pl_el"][k:k + 1])
+        pr.append(a[0]); pv.append(b[0])
+    r, v = G.elements_to_cartesian(m[0], el)
+    return w, m, np.array(pr), np.array(pv), r, v
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            if len(r) > 8:
+                for k, nm in enumerate(names):
+                    if r[5 + k].lower().startswith("active"):
+                        reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(sample_n, sample_steps, state, block, dt, outer, threads):
+    """The oracle's restatement of the reference kernel (src/wh.cu:113-177)
+    over a particle sample, split across host threads (ctypes releases the GIL)."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import oracle as O
+    O.lib()
+    r, v, a = state
+    r = np.ascontiguousarray(r[:sample_n]); v = np.ascontiguousarray(v[:sample_n]); a = np.ascontiguousarray(a[:sample_n])
+    npl = len(block["m"])
+    h0 = np.ascontiguousarray(block["h0_log"][:sample_steps])
+    rl = np.ascontiguousarray(block["r_log"][:sample_steps])
+    chunks = np.array_split(np.arange(sample_n), threads)
+
+    def work(idx):
+        rr, vv, aa = r[idx].copy(), v[idx].copy(), a[idx].copy()
+        O.block(rr, vv, aa, np.zeros(len(idx), np.uint16), sample_steps, npl, h0, rl, block["m"], block["id"],
+                block["rh"], outer, dt, float(block["m"][0]), drift="mvs")
+        return len(idx)
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as pool:
+        done = sum(pool.map(work, chunks))
+    el = time.perf_counter() - t0
+    return done * sample_steps / el, el
+
+
+def run_reference_arm(args, rank, world):
+    """CPU implementation of the path (the oracle port of the reference
+    kernel) on the host cores: same metric, config and unit as the GPU arm."""
+    if rank != 0:
+        return
+    import glisser_gb300 as G
+    from oracle import oracle as O
+    G.build()
+    O.build()
+    n_planets = 4
+    w, m, pr, pv, r, v = make_state(G, args.sample_particles, 2, 0)
+    ex = O.Exec(m, pr, pv, np.arange(len(m)), r, v, np.arange(len(r)), dt=180.0, tbsize=args.sample_steps)
+    p = ex.particles()
+    blk = ex.planet_block()
+    threads = os.cpu_count() or 1
+    vals = []
+    for k in range(args.warmup + args.steps):
+        val, el = cpu_baseline(args.sample_particles, args.sample_steps, (p["r"], p["v"], p["a"]), blk, 180.0, 300.0,
+                               threads)
+        if k >= args.warmup:
+            vals.append((val, el))
+    value = len(vals) * args.sample_particles * args.sample_steps / sum(e for _, e in vals)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * sum(e for _, e in vals) / len(vals), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "plain-giants: Sun + 4 giants, particles a~U(53,57) au e~U(0,0.3) i~U(0,10deg), "
+                               "dt=180 d, T=2048 (CPU sample per step: %d particles x %d steps)"
+                               % (args.sample_particles, args.sample_steps),
+                   "n_planets": n_planets, "l2": "n/a (host CPU)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "%d particles x %d steps per step, oracle restatement of MVSKernel::step_forward "
+                                   "(src/wh.cu:113-177), %d host threads" % (args.sample_particles, args.sample_steps,
+                                                                             threads)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="glisser", choices=["glisser", "reference"])
+    ap.add_argument("--particles", type=int, default=1_000_000)
+    ap.add_argument("--tbsize", type=int, default=2048)
+    ap.add_argument("--starter", default="series", choices=["classic", "series", "learned"])
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--sample-particles", type=int, default=65536)
+    ap.add_argument("--sample-steps", type=int, default=512)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference_arm(args, rank, world)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import glisser_gb300 as G
+    G.build()
+    starter = {"classic": G.STARTER_CLASSIC, "series": G.STARTER_SERIES, "learned": G.STARTER_LEARNED}[args.starter]
+
+    w, m, pr, pv, r, v = make_state(G, args.particles, 2, rank)
+    n_planets = len(m) - 1
+    dt = 180.0
+    sim = G.Simulation(config_text(args.tbsize, dt))
+    sim.set_planets(m, pr, pv)
+    sim.set_particles(r, v)
+    sim.set_starter(starter, os.path.join(ROOT, "glisser_gb300", "weights", "starter.bin")
+                    if starter == G.STARTER_LEARNED else None)
+    sim.init()
+    blk0 = sim.planet_block()
+    stream = torch.cuda.ExternalStream(sim.stream(), device=torch.device("cuda", local))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # 256 MB > L2
+
+    peak_tf, _ = G.fp64_peak_probe()
+    for _ in range(args.warmup):
+        sim.loop()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    barrier()
+    clocks.start()
+    s0 = sim.stats()
+    e_start = torch.cuda.Event(enable_timing=True)
+    e_stop = torch.cuda.Event(enable_timing=True)
+    e_start.record(stream)
+    kernel_ms = []
+    psteps = []
+    for k in range(args.steps):
+        before = sim.stats()["particle_steps"]
+        _, _, gms = sim.loop()
+        kernel_ms.append(gms)
+        psteps.append(sim.stats()["particle_steps"] - before)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+    e_stop.record(stream)
+    e_stop.synchronize()
+    barrier()
+    clk = clocks.stop()
+    elapsed_ms = e_start.elapsed_time(e_stop)
+    s1 = sim.stats()
+    total_ps = s1["particle_steps"] - s0["particle_steps"]
+    launches = s1["launches"] - s0["launches"]
+    if dist is not None:
+        t = torch.tensor([elapsed_ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+        ps = torch.tensor([float(total_ps)], dtype=torch.float64, device="cuda")
+        dist.all_reduce(ps, op=dist.ReduceOp.SUM)
+        total_ps_all = float(ps.item())
+    else:
+        total_ps_all = float(total_ps)
+    value = total_ps_all / (elapsed_ms * 1e-3)
+
+    F = alg_flops_per_particle_step(n_planets)
+    achieved_tf = sum(p * F for p in psteps) / (sum(kernel_ms) * 1e-3) / 1e12
+    traffic = None
+    tf_path = os.path.join(ROOT, "profiles", "timeblock_traffic.json")
+    if os.path.exists(tf_path):
+        with open(tf_path) as f:
+            tinfo = json.load(f)
+        traffic = tinfo.get("dram_bytes_per_particle_block", 0) * (sum(psteps) / len(psteps)) / args.tbsize
+
+    # end to end through the C ABI with host buffers
+    e2e = None
+    if args.e2e_steps > 0:
+        host = sim.particles()
+        rr, vv = host["r"].copy(), host["v"].copy()
+        nn = len(rr)
+        barrier()
+        t0 = time.perf_counter()
+        ps0 = sim.stats()["particle_steps"]
+        for _ in range(args.e2e_steps):
+            sim.set_particles(rr, vv)           # H2D of this block's inputs
+            sim.loop()
+            out = sim.particles()               # D2H of the block's result
+            rr, vv = out["r"], out["v"]
+        barrier()
+        el = time.perf_counter() - t0
+        eps = (sim.stats()["particle_steps"] - ps0)
+        if dist is not None:
+            tt = torch.tensor([el, float(eps)], dtype=torch.float64, device="cuda")
+            dist.all_reduce(tt[:1], op=dist.ReduceOp.MAX)
+            dist.all_reduce(tt[1:], op=dist.ReduceOp.SUM)
+            el, eps = float(tt[0].item()), float(tt[1].item())
+        log_bytes = args.tbsize * (n_planets + 1) * 24 + 3 * (n_planets + 1) * 8
+        e2e = {"value": eps / el, "unit": UNIT, "h2d_bytes_per_step": nn * 48 + log_bytes,
+               "d2h_bytes_per_step": nn * (48 + 4 + 4 + 2) + 72}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        st = sim.particles()
+        # the kernel's accelerations are not exported; recompute them as the
+        # reference does at start (helio_acc_particle) by stepping the oracle
+        from oracle import oracle as O
+        n_s = min(args.sample_particles, len(st["r"]))
+        ex = O.Exec(m, pr, pv, np.arange(len(m)), r[:n_s], v[:n_s], np.arange(n_s), dt=dt, tbsize=args.sample_steps)
+        po = ex.particles()
+        threads = os.cpu_count() or 1
+        val, el = cpu_baseline(n_s, args.sample_steps, (po["r"], po["v"], po["a"]), ex.planet_block(), dt, 300.0,
+                               threads)
+        cpu = {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "%d particles x %d steps (%.1f s), oracle restatement of MVSKernel::step_forward "
+                         "(src/wh.cu:113-177) on %d host threads" % (n_s, args.sample_steps, el, threads)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "plain-giants: Sun + 4 giants (masses 9.55e-4, 2.86e-4, 4.37e-5, 5.15e-5 Msun), "
+                                   "%d particles per GPU near the Neptune 3:1, a~U(53,57) au, e~U(0,0.3), "
+                                   "i~U(0,10deg), FP64, dt=180 d, Time-Block-Size %d; one step = one time block"
+                                   % (args.particles, args.tbsize),
+                       "particles_per_gpu": args.particles, "time_block": args.tbsize, "n_planets": n_planets,
+                       "starter": args.starter, "parallelism": "independent particle shards per GPU",
+                       "l2": "flushed between timed blocks (256 MB write)"},
+            "roofline": {"bound": "fp64", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
+                         "frac": achieved_tf / peak_tf if peak_tf else None, "traffic": traffic,
+                         "kernel": "timeblock_kernel", "flops_per_particle_step": F,
+                         "peak_source": "measured FP64 DFMA probe (glisser_fp64_peak_probe); MEASURED_PEAKS.json "
+                                        "has no FP64 figure"},
+            "kernel_ms_per_block": sum(kernel_ms) / len(kernel_ms),
+            "particle_steps_per_block": sum(psteps) / len(psteps),
+            "kepler_evals_per_particle_step": (s1["kepler_evals"] - s0["kepler_evals"]) / max(total_ps, 1),
+            "gpu_launches": launches,
+            "clocks": clk,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

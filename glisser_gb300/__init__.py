@@ -1,0 +1,337 @@
+"""glisser-gb300: the massless-particle Wisdom-Holman/MVS time-block integrator
+of glisser, rebuilt for GB300 (sm_103a).
+
+Python front-end over the C ABI in include/glisser.h (loaded with ctypes).
+`Simulation` mirrors sr::exec::ExecutorFacade (src/executor_facade.h:18-39);
+`integrate_timeblock` is the device-level seam
+WHCudaIntegrator::integrate_particles_timeblock_cuda (src/wh.cuh:51-57).
+There is no CPU fallback: without the compiled library every call raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libglisser_gb300.so")
+
+OK = 0
+E_INVALID, E_CONFIG, E_IO, E_CUDA, E_STATE, E_NOMEM, E_EOS, E_RUNTIME, E_TIMEOUT = range(-1, -10, -1)
+STARTER_CLASSIC, STARTER_SERIES, STARTER_LEARNED = 0, 1, 2
+FLAG_ENCOUNTER, FLAG_OUT_OF_BOUNDS, FLAG_KEPLER, FLAG_UNBOUND, FLAG_DEAD = 0x01, 0x02, 0x04, 0x08, 0x80
+
+
+class GlisserError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (code %d)" % (msg, code))
+        self.code = code
+
+
+class ConfigError(GlisserError):
+    pass
+
+
+class EndOfHistory(GlisserError):
+    pass
+
+
+D = C.POINTER(C.c_double)
+U32 = C.POINTER(C.c_uint32)
+U16 = C.POINTER(C.c_uint16)
+SZ = C.POINTER(C.c_size_t)
+
+
+class ParticlesDev(C.Structure):
+    """glisser_particles: device pointers of the SoA particle state."""
+    _fields_ = [(k, C.c_void_p) for k in ("rx", "ry", "rz", "vx", "vy", "vz", "ax", "ay", "az", "flags",
+                                          "deathtime_index", "id")]
+
+
+class PlanetBlockDev(C.Structure):
+    _fields_ = [("log", C.c_void_p), ("m", C.c_void_p), ("id", C.c_void_p), ("rh", C.c_void_p),
+                ("npl", C.c_uint32), ("len", C.c_uint32), ("capacity", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class StepParams(C.Structure):
+    _fields_ = [("dt", C.c_double), ("outer_radius", C.c_double), ("starter", C.c_int32),
+                ("kill_encounters", C.c_int32), ("mlp", C.c_void_p)]
+
+
+class HandoffDev(C.Structure):
+    _fields_ = [("count", C.c_void_p), ("index", C.c_void_p), ("id", C.c_void_p), ("flags", C.c_void_p),
+                ("deathtime_index", C.c_void_p), ("capacity", C.c_uint32), ("reserved", C.c_uint32),
+                ("status", C.c_void_p), ("evals", C.c_void_p)]
+
+
+_lib = None
+
+
+def build(verbose=False):
+    """Compiles the native library in-tree (sm_103a) if it is out of date."""
+    from . import native_build
+    return native_build.build(verbose=verbose)
+
+
+def lib():
+    """The native library; raises when it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("glisser_gb300 native library missing (%s): run glisser_gb300.build()" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        P = C.c_void_p
+        sig = {
+            "glisser_create": ([C.c_char_p, C.POINTER(P)], C.c_int),
+            "glisser_destroy": ([P], C.c_int),
+            "glisser_last_error": ([P, C.c_char_p, C.c_size_t], C.c_int),
+            "glisser_last_error_global": ([C.c_char_p, C.c_size_t], C.c_int),
+            "glisser_config_get": ([P, C.c_char_p, C.c_char_p, C.c_size_t], C.c_int),
+            "glisser_write_config": ([P, C.c_char_p, C.c_double, C.c_double], C.c_int),
+            "glisser_load_state": ([P], C.c_int),
+            "glisser_set_planets": ([P, C.c_size_t, D, D, D, U32], C.c_int),
+            "glisser_set_particles": ([P, C.c_size_t, D, D, U32, U16, D], C.c_int),
+            "glisser_set_starter": ([P, C.c_int, C.c_char_p], C.c_int),
+            "glisser_init": ([P], C.c_int),
+            "glisser_step_block": ([P, C.POINTER(C.c_int), D, D], C.c_int),
+            "glisser_run": ([P, C.c_int], C.c_int),
+            "glisser_finish": ([P], C.c_int),
+            "glisser_time": ([P, D], C.c_int),
+            "glisser_energy0": ([P, D], C.c_int),
+            "glisser_counts": ([P, SZ, SZ, SZ], C.c_int),
+            "glisser_get_particles": ([P, D, D, U32, U16, D, U32, C.c_size_t, SZ], C.c_int),
+            "glisser_get_planets": ([P, D, D, D, U32, C.c_size_t, SZ], C.c_int),
+            "glisser_get_planet_block": ([P, D, D, U32, D, C.c_uint32, U32, U32], C.c_int),
+            "glisser_get_flagged": ([P, U32, U16, U32, C.c_size_t, SZ], C.c_int),
+            "glisser_write_state": ([P, C.c_char_p, C.c_int], C.c_int),
+            "glisser_write_track": ([P, C.c_char_p, C.c_int], C.c_int),
+            "glisser_write_plhist": ([P, C.c_char_p, C.c_int], C.c_int),
+            "glisser_from_elements_M": ([C.c_double] * 7 + [D, D], C.c_int),
+            "glisser_to_elements": ([C.c_double, D, D, C.POINTER(C.c_int), D], C.c_int),
+            "glisser_integrate_timeblock": ([C.POINTER(ParticlesDev), C.c_size_t, C.POINTER(PlanetBlockDev),
+                                             C.POINTER(StepParams), C.POINTER(HandoffDev), P], C.c_int),
+            "glisser_partition_scratch_bytes": ([C.c_size_t], C.c_size_t),
+            "glisser_partition": ([C.POINTER(ParticlesDev), C.POINTER(ParticlesDev), C.c_size_t, P, P, P, P], C.c_int),
+            "glisser_stats": ([P, C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong)], C.c_int),
+            "glisser_elements_to_cartesian": ([C.c_size_t, C.c_double, D, D, D], C.c_int),
+            "glisser_fp64_peak_probe": ([D, D], C.c_int),
+            "glisser_launches": ([P, C.POINTER(C.c_ulonglong)], C.c_int),
+            "glisser_stream": ([P, C.POINTER(P)], C.c_int),
+        }
+        for name, (args, res) in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+def _p(a, t):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+def last_error():
+    buf = C.create_string_buffer(1024)
+    lib().glisser_last_error_global(buf, 1024)
+    return buf.value.decode(errors="replace")
+
+
+def _raise(code, msg):
+    if code == E_CONFIG:
+        raise ConfigError(code, msg)
+    if code == E_EOS:
+        raise EndOfHistory(code, msg)
+    raise GlisserError(code, msg)
+
+
+def from_elements_M(mu, a, e, i, capom, om, M):
+    r = np.zeros(3)
+    v = np.zeros(3)
+    lib().glisser_from_elements_M(mu, a, e, i, capom, om, M, _p(r, D), _p(v, D))
+    return r, v
+
+
+def elements_to_cartesian(mu, el):
+    """[n, 6] elements (a, e, i, capom, om, M) -> r, v [n, 3]."""
+    el = np.ascontiguousarray(el, np.float64)
+    r = np.zeros((len(el), 3))
+    v = np.zeros((len(el), 3))
+    rc = lib().glisser_elements_to_cartesian(len(el), mu, _p(el, D), _p(r, D), _p(v, D))
+    if rc:
+        _raise(rc, last_error())
+    return r, v
+
+
+def fp64_peak_probe():
+    """Measured FP64 FMA throughput of cuda:0 in TFLOP/s (and the probe's ms)."""
+    tf, ms = C.c_double(), C.c_double()
+    rc = lib().glisser_fp64_peak_probe(C.byref(tf), C.byref(ms))
+    if rc:
+        _raise(rc, last_error())
+    return tf.value, ms.value
+
+
+def to_elements(mu, r, v):
+    out = np.zeros(6)
+    es = C.c_int()
+    lib().glisser_to_elements(mu, _p(np.ascontiguousarray(r, np.float64), D),
+                              _p(np.ascontiguousarray(v, np.float64), D), C.byref(es), _p(out, D))
+    return es.value, out
+
+
+class Simulation:
+    """One run of the block integrator (ExecutorFacade)."""
+
+    def __init__(self, config_text):
+        h = C.c_void_p()
+        rc = lib().glisser_create(config_text.encode(), C.byref(h))
+        if rc:
+            _raise(rc, last_error())
+        self.h = h
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h and _lib is not None:
+            _lib.glisser_destroy(h)
+            self.h = None
+
+    def _check(self, rc):
+        if rc:
+            buf = C.create_string_buffer(2048)
+            lib().glisser_last_error(self.h, buf, 2048)
+            _raise(rc, buf.value.decode(errors="replace"))
+
+    def config(self, key):
+        buf = C.create_string_buffer(4096)
+        self._check(lib().glisser_config_get(self.h, key.encode(), buf, 4096))
+        return buf.value.decode()
+
+    def write_config(self, path, t0, tf):
+        self._check(lib().glisser_write_config(self.h, path.encode(), t0, tf))
+
+    def load_state(self):
+        self._check(lib().glisser_load_state(self.h))
+
+    def set_planets(self, m, r, v, ids=None):
+        m = np.ascontiguousarray(m, np.float64)
+        r = np.ascontiguousarray(r, np.float64)
+        v = np.ascontiguousarray(v, np.float64)
+        ids = None if ids is None else np.ascontiguousarray(ids, np.uint32)
+        self._check(lib().glisser_set_planets(self.h, len(m), _p(m, D), _p(r, D), _p(v, D), _p(ids, U32)))
+
+    def set_particles(self, r, v, ids=None, flags=None, deathtime=None):
+        r = np.ascontiguousarray(r, np.float64)
+        v = np.ascontiguousarray(v, np.float64)
+        ids = None if ids is None else np.ascontiguousarray(ids, np.uint32)
+        flags = None if flags is None else np.ascontiguousarray(flags, np.uint16)
+        deathtime = None if deathtime is None else np.ascontiguousarray(deathtime, np.float64)
+        self._check(lib().glisser_set_particles(self.h, len(r), _p(r, D), _p(v, D), _p(ids, U32), _p(flags, U16),
+                                                _p(deathtime, D)))
+
+    def set_starter(self, starter, mlp_path=None):
+        self._check(lib().glisser_set_starter(self.h, starter, mlp_path.encode() if mlp_path else None))
+
+    def init(self):
+        self._check(lib().glisser_init(self.h))
+
+    def loop(self):
+        """One time block; returns (safe_to_output, cpu_ms, gpu_ms)."""
+        safe = C.c_int()
+        cpu, gpu = C.c_double(), C.c_double()
+        self._check(lib().glisser_step_block(self.h, C.byref(safe), C.byref(cpu), C.byref(gpu)))
+        return bool(safe.value), cpu.value, gpu.value
+
+    def run(self, quiet=True, force=False):
+        self._check(lib().glisser_run(self.h, (1 if quiet else 0) | (2 if force else 0)))
+
+    def finish(self):
+        self._check(lib().glisser_finish(self.h))
+
+    @property
+    def t(self):
+        x = C.c_double()
+        lib().glisser_time(self.h, C.byref(x))
+        return x.value
+
+    @property
+    def e_0(self):
+        x = C.c_double()
+        lib().glisser_energy0(self.h, C.byref(x))
+        return x.value
+
+    def counts(self):
+        n, na, ne = C.c_size_t(), C.c_size_t(), C.c_size_t()
+        lib().glisser_counts(self.h, C.byref(n), C.byref(na), C.byref(ne))
+        return dict(n=n.value, n_alive=na.value, n_encounter=ne.value)
+
+    def stats(self):
+        ps, ev, ln = C.c_ulonglong(), C.c_ulonglong(), C.c_ulonglong()
+        lib().glisser_stats(self.h, C.byref(ps), C.byref(ev))
+        lib().glisser_launches(self.h, C.byref(ln))
+        return dict(particle_steps=ps.value, kepler_evals=ev.value, launches=ln.value)
+
+    def stream(self):
+        s = C.c_void_p()
+        lib().glisser_stream(self.h, C.byref(s))
+        return s.value or 0
+
+    def particles(self):
+        n = self.counts()["n"]
+        r = np.zeros((n, 3)); v = np.zeros((n, 3))
+        ids = np.zeros(n, np.uint32); fl = np.zeros(n, np.uint16); dt = np.zeros(n); dti = np.zeros(n, np.uint32)
+        got = C.c_size_t()
+        self._check(lib().glisser_get_particles(self.h, _p(r, D), _p(v, D), _p(ids, U32), _p(fl, U16), _p(dt, D),
+                                                _p(dti, U32), n, C.byref(got)))
+        return dict(r=r, v=v, id=ids, flags=fl, deathtime=dt, deathtime_index=dti)
+
+    def planets(self, cap=64):
+        m = np.zeros(cap); r = np.zeros((cap, 3)); v = np.zeros((cap, 3)); ids = np.zeros(cap, np.uint32)
+        n = C.c_size_t()
+        self._check(lib().glisser_get_planets(self.h, _p(m, D), _p(r, D), _p(v, D), _p(ids, U32), cap, C.byref(n)))
+        k = n.value
+        return dict(m=m[:k], r=r[:k], v=v[:k], id=ids[:k])
+
+    def planet_block(self, cap_steps=1 << 16):
+        npl, ln = C.c_uint32(), C.c_uint32()
+        self._check(lib().glisser_get_planet_block(self.h, None, None, None, None, 0xFFFFFFFF, C.byref(npl),
+                                                   C.byref(ln)))
+        k, L = npl.value, ln.value
+        log = np.zeros((L, k, 3)); m = np.zeros(k); ids = np.zeros(k, np.uint32); rh = np.zeros(k)
+        self._check(lib().glisser_get_planet_block(self.h, _p(log, D), _p(m, D), _p(ids, U32), _p(rh, D), L,
+                                                   C.byref(npl), C.byref(ln)))
+        return dict(h0_log=log[:, 0, :], r_log=log[:, 1:, :], m=m, id=ids, rh=rh, npl=k, log_len=L)
+
+    def flagged(self):
+        n = C.c_size_t()
+        lib().glisser_get_flagged(self.h, None, None, None, 0, C.byref(n))
+        k = n.value
+        ids = np.zeros(k, np.uint32); fl = np.zeros(k, np.uint16); dti = np.zeros(k, np.uint32)
+        self._check(lib().glisser_get_flagged(self.h, _p(ids, U32), _p(fl, U16), _p(dti, U32), k, C.byref(n)))
+        return dict(id=ids, flags=fl, deathtime_index=dti)
+
+    def write_state(self, path, binary=False):
+        self._check(lib().glisser_write_state(self.h, path.encode(), int(binary)))
+
+    def write_track(self, path, append=False):
+        self._check(lib().glisser_write_track(self.h, path.encode(), int(append)))
+
+    def write_plhist(self, path, begin=False):
+        self._check(lib().glisser_write_plhist(self.h, path.encode(), int(begin)))
+
+
+def integrate_timeblock(particles, n_alive, planet_block, params, handoff, stream=0):
+    """Kernel-level entry (device pointers in the ctypes structs)."""
+    rc = lib().glisser_integrate_timeblock(C.byref(particles), n_alive, C.byref(planet_block), C.byref(params),
+                                           C.byref(handoff), C.c_void_p(stream))
+    if rc:
+        _raise(rc, last_error())
+
+
+def partition(src, dst, n, scratch, n0_ptr, n1_ptr, stream=0):
+    rc = lib().glisser_partition(C.byref(src), C.byref(dst), n, C.c_void_p(scratch), C.c_void_p(n0_ptr),
+                                 C.c_void_p(n1_ptr), C.c_void_p(stream))
+    if rc:
+        _raise(rc, last_error())
+
+
+def partition_scratch_bytes(n):
+    return lib().glisser_partition_scratch_bytes(n)

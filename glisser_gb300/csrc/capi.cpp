@@ -1,0 +1,436 @@
+// extern "C" boundary: every entry point catches, maps the exception type to
+// a GLISSER_E_* code and keeps the message for glisser_last_error.
+#include <algorithm>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <new>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "../../include/glisser.h"
+#include "config.h"
+#include "executor.h"
+#include "orbits.h"
+#include "state_io.h"
+#include "timeblock.cuh"
+
+namespace glisser {
+size_t partition_scratch_bytes(size_t n);
+int launch_partition(const glisser_particles* in, const glisser_particles* out, size_t n, void* scratch,
+                     uint32_t* n0, uint32_t* n1, cudaStream_t stream);
+size_t mlp_blob_bytes();
+}  // namespace glisser
+
+struct glisser_s {
+    std::unique_ptr<glisser::Executor> ex;
+    std::string err;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int code_for(const std::exception& e)
+{
+    if (dynamic_cast<const glisser::ConfigError*>(&e)) return GLISSER_E_CONFIG;
+    if (dynamic_cast<const glisser::IoError*>(&e)) return GLISSER_E_IO;
+    if (dynamic_cast<const glisser::CudaError*>(&e)) return GLISSER_E_CUDA;
+    if (dynamic_cast<const glisser::EndOfHistory*>(&e)) return GLISSER_E_EOS;
+    if (dynamic_cast<const glisser::StateError*>(&e)) return GLISSER_E_STATE;
+    if (dynamic_cast<const std::bad_alloc*>(&e)) return GLISSER_E_NOMEM;
+    if (dynamic_cast<const std::invalid_argument*>(&e)) return GLISSER_E_INVALID;
+    return GLISSER_E_RUNTIME;
+}
+
+template <typename F>
+int guarded(glisser_t* h, F&& f)
+{
+    try {
+        return f();
+    } catch (const std::exception& e) {
+        std::string msg = e.what();
+        if (h) h->err = msg;
+        g_last_error = msg;
+        return code_for(e);
+    } catch (...) {
+        if (h) h->err = "unknown error";
+        g_last_error = "unknown error";
+        return GLISSER_E_RUNTIME;
+    }
+}
+
+int fail(glisser_t* h, int code, const std::string& msg)
+{
+    if (h) h->err = msg;
+    g_last_error = msg;
+    return code;
+}
+
+int copy_text(const std::string& s, char* buf, size_t cap)
+{
+    if (!buf || cap == 0) return GLISSER_E_INVALID;
+    size_t k = std::min(cap - 1, s.size());
+    std::memcpy(buf, s.data(), k);
+    buf[k] = 0;
+    return GLISSER_OK;
+}
+
+glisser::Executor& exec_of(glisser_t* h)
+{
+    if (!h || !h->ex) throw std::invalid_argument("null handle");
+    return *h->ex;
+}
+
+}  // namespace
+
+extern "C" {
+
+int glisser_integrate_timeblock(const glisser_particles* pa, size_t n_alive, const glisser_planet_block* pl,
+                                const glisser_step_params* sp, const glisser_handoff* ho, void* stream)
+{
+    int rc = glisser::launch_timeblock(pa, n_alive, pl, sp, ho, (cudaStream_t)stream);
+    if (rc == GLISSER_E_INVALID) g_last_error = "glisser_integrate_timeblock: invalid argument";
+    else if (rc != GLISSER_OK) g_last_error = glisser::timeblock_error();
+    return rc;
+}
+
+size_t glisser_partition_scratch_bytes(size_t n) { return glisser::partition_scratch_bytes(n); }
+
+int glisser_partition(const glisser_particles* in, const glisser_particles* out, size_t n, void* scratch,
+                      uint32_t* n_unflagged, uint32_t* n_encounter, void* stream)
+{
+    int rc = glisser::launch_partition(in, out, n, scratch, n_unflagged, n_encounter, (cudaStream_t)stream);
+    if (rc != GLISSER_OK) g_last_error = "glisser_partition failed";
+    return rc;
+}
+
+int glisser_last_error_global(char* buf, size_t cap) { return copy_text(g_last_error, buf, cap); }
+
+int glisser_last_error(const glisser_t* h, char* buf, size_t cap)
+{
+    if (!h) return copy_text(g_last_error, buf, cap);
+    return copy_text(h->err, buf, cap);
+}
+
+int glisser_create(const char* config_text, glisser_t** out)
+{
+    if (!config_text || !out) return fail(nullptr, GLISSER_E_INVALID, "glisser_create: null argument");
+    *out = nullptr;
+    return guarded(nullptr, [&] {
+        std::string warnings;
+        glisser::Config cfg = glisser::parse_config(config_text, &warnings);
+        std::unique_ptr<glisser_s> h(new glisser_s());
+        h->ex.reset(new glisser::Executor(cfg));
+        h->ex->warnings = warnings;
+        *out = h.release();
+        return GLISSER_OK;
+    });
+}
+
+int glisser_destroy(glisser_t* h)
+{
+    delete h;
+    return GLISSER_OK;
+}
+
+int glisser_config_get(const glisser_t* h, const char* key, char* buf, size_t cap)
+{
+    if (!h || !key) return GLISSER_E_INVALID;
+    std::string v;
+    if (!glisser::config_get(h->ex->cfg, key, v)) return fail(const_cast<glisser_t*>(h), GLISSER_E_INVALID, "unknown key");
+    return copy_text(v, buf, cap);
+}
+
+int glisser_write_config(const glisser_t* h, const char* path, double t0, double tf)
+{
+    glisser_t* hh = const_cast<glisser_t*>(h);
+    return guarded(hh, [&] {
+        glisser::Config c = exec_of(hh).cfg;
+        c.t_0 = t0;
+        c.t_f = tf;
+        std::ofstream o(path);
+        if (!o) throw glisser::IoError(std::string("cannot write ") + path);
+        o << glisser::format_config(c);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_load_state(glisser_t* h)
+{
+    return guarded(h, [&] {
+        exec_of(h).load();
+        return GLISSER_OK;
+    });
+}
+
+int glisser_set_planets(glisser_t* h, size_t n, const double* m, const double* r, const double* v, const uint32_t* id)
+{
+    if (n < 1 || !m || !r || !v) return fail(h, GLISSER_E_INVALID, "glisser_set_planets: bad arguments");
+    return guarded(h, [&] {
+        exec_of(h).set_planets(n, m, r, v, id);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_set_particles(glisser_t* h, size_t n, const double* r, const double* v, const uint32_t* id,
+                          const uint16_t* flags, const double* deathtime)
+{
+    if ((n && (!r || !v))) return fail(h, GLISSER_E_INVALID, "glisser_set_particles: bad arguments");
+    return guarded(h, [&] {
+        exec_of(h).set_particles(n, r, v, id, flags, deathtime);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_set_starter(glisser_t* h, int starter, const char* mlp_path)
+{
+    return guarded(h, [&] {
+        std::vector<uint8_t> blob;
+        if (mlp_path) {
+            std::ifstream in(mlp_path, std::ios::binary);
+            if (!in) throw glisser::IoError(std::string("cannot read ") + mlp_path);
+            blob.assign(std::istreambuf_iterator<char>(in), std::istreambuf_iterator<char>());
+        }
+        exec_of(h).set_starter(starter, mlp_path ? &blob : nullptr);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_init(glisser_t* h)
+{
+    return guarded(h, [&] {
+        exec_of(h).init();
+        return GLISSER_OK;
+    });
+}
+
+int glisser_step_block(glisser_t* h, int* safe_to_output, double* cpu_ms, double* gpu_ms)
+{
+    return guarded(h, [&] {
+        bool safe = exec_of(h).step_block(cpu_ms, gpu_ms);
+        if (safe_to_output) *safe_to_output = safe ? 1 : 0;
+        return GLISSER_OK;
+    });
+}
+
+int glisser_run(glisser_t* h, int quiet)
+{
+    return guarded(h, [&] {
+        std::string err;
+        int rc = glisser::run_main(exec_of(h), (quiet & 1) != 0, (quiet & 2) != 0, err);
+        if (rc == -2) return fail(h, GLISSER_E_IO, err);
+        if (rc != 0) return fail(h, GLISSER_E_RUNTIME, err);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_finish(glisser_t* h)
+{
+    return guarded(h, [&] {
+        exec_of(h).finish();
+        return GLISSER_OK;
+    });
+}
+
+int glisser_time(const glisser_t* h, double* t)
+{
+    if (!h || !t) return GLISSER_E_INVALID;
+    *t = h->ex->t;
+    return GLISSER_OK;
+}
+
+int glisser_energy0(const glisser_t* h, double* e0)
+{
+    if (!h || !e0) return GLISSER_E_INVALID;
+    *e0 = h->ex->e0;
+    return GLISSER_OK;
+}
+
+int glisser_counts(const glisser_t* h, size_t* n, size_t* n_alive, size_t* n_encounter)
+{
+    if (!h) return GLISSER_E_INVALID;
+    if (n) *n = h->ex->n_total();
+    if (n_alive) *n_alive = h->ex->n_alive_host();
+    if (n_encounter) *n_encounter = h->ex->n_encounter();
+    return GLISSER_OK;
+}
+
+int glisser_get_particles(const glisser_t* h, double* r, double* v, uint32_t* id, uint16_t* flags, double* deathtime,
+                          uint32_t* deathtime_index, size_t cap, size_t* n)
+{
+    glisser_t* hh = const_cast<glisser_t*>(h);
+    return guarded(hh, [&] {
+        const glisser::Particles& pa = exec_of(hh).particles();
+        if (n) *n = pa.n;
+        if (cap < pa.n) return fail(hh, GLISSER_E_INVALID, "glisser_get_particles: buffer too small");
+        for (size_t k = 0; k < pa.n; k++) {
+            if (r) { r[3 * k] = pa.r[k].x; r[3 * k + 1] = pa.r[k].y; r[3 * k + 2] = pa.r[k].z; }
+            if (v) { v[3 * k] = pa.v[k].x; v[3 * k + 1] = pa.v[k].y; v[3 * k + 2] = pa.v[k].z; }
+            if (id) id[k] = pa.id[k];
+            if (flags) flags[k] = pa.flags[k];
+            if (deathtime) deathtime[k] = pa.deathtime[k];
+            if (deathtime_index) deathtime_index[k] = pa.deathtime_index[k];
+        }
+        return GLISSER_OK;
+    });
+}
+
+int glisser_get_planets(const glisser_t* h, double* m, double* r, double* v, uint32_t* id, size_t cap, size_t* n)
+{
+    glisser_t* hh = const_cast<glisser_t*>(h);
+    return guarded(hh, [&] {
+        glisser::Executor& ex = exec_of(hh);
+        const glisser::Planets& pl = ex.initialized() ? ex.planets_snapshot() : ex.planets_live();
+        if (n) *n = pl.n_alive;
+        if (cap < pl.n_alive) return fail(hh, GLISSER_E_INVALID, "glisser_get_planets: buffer too small");
+        for (size_t k = 0; k < pl.n_alive; k++) {
+            if (m) m[k] = pl.m[k];
+            if (r) { r[3 * k] = pl.r[k].x; r[3 * k + 1] = pl.r[k].y; r[3 * k + 2] = pl.r[k].z; }
+            if (v) { v[3 * k] = pl.v[k].x; v[3 * k + 1] = pl.v[k].y; v[3 * k + 2] = pl.v[k].z; }
+            if (id) id[k] = pl.id[k];
+        }
+        return GLISSER_OK;
+    });
+}
+
+int glisser_get_flagged(const glisser_t* h, uint32_t* ids, uint16_t* flags, uint32_t* deathtime_index, size_t cap,
+                        size_t* n)
+{
+    if (!h) return GLISSER_E_INVALID;
+    const auto& f = h->ex->last_flagged();
+    if (n) *n = f.size();
+    size_t k = std::min(cap, f.size());
+    for (size_t q = 0; q < k; q++) {
+        if (ids) ids[q] = f[q].id;
+        if (flags) flags[q] = f[q].flags;
+        if (deathtime_index) deathtime_index[q] = f[q].deathtime_index;
+    }
+    return cap < f.size() ? GLISSER_E_INVALID : GLISSER_OK;
+}
+
+int glisser_get_planet_block(const glisser_t* h, double* log, double* m, uint32_t* id, double* rh, uint32_t cap_steps,
+                             uint32_t* npl, uint32_t* len)
+{
+    glisser_t* hh = const_cast<glisser_t*>(h);
+    return guarded(hh, [&] {
+        glisser::Executor& ex = exec_of(hh);
+        if (!ex.initialized()) return fail(hh, GLISSER_E_INVALID, "no planet block before init");
+        std::vector<double> lg, mm, rr;
+        std::vector<uint32_t> ii;
+        uint32_t np = 0, ln = 0;
+        ex.planet_block(lg, mm, ii, rr, np, ln);
+        if (npl) *npl = np;
+        if (len) *len = ln;
+        if (cap_steps < ln) return fail(hh, GLISSER_E_INVALID, "glisser_get_planet_block: buffer too small");
+        if (log) std::copy(lg.begin(), lg.end(), log);
+        if (m) std::copy(mm.begin(), mm.end(), m);
+        if (id) std::copy(ii.begin(), ii.end(), id);
+        if (rh) std::copy(rr.begin(), rr.end(), rh);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_write_state(const glisser_t* h, const char* path, int binary)
+{
+    glisser_t* hh = const_cast<glisser_t*>(h);
+    return guarded(hh, [&] {
+        glisser::Executor& ex = exec_of(hh);
+        glisser::Config c = ex.cfg;
+        c.writesplit = false;
+        c.writebinary = binary != 0;
+        const glisser::Planets& pl = ex.initialized() ? ex.planets_snapshot() : ex.planets_live();
+        glisser::save_state(c, pl, ex.particles(), path);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_write_track(const glisser_t* h, const char* path, int append)
+{
+    glisser_t* hh = const_cast<glisser_t*>(h);
+    return guarded(hh, [&] {
+        glisser::Executor& ex = exec_of(hh);
+        std::ofstream out(path, append ? (std::ios::binary | std::ios::app) : std::ios::binary);
+        if (!out) throw glisser::IoError(std::string("cannot write ") + path);
+        const glisser::Particles& pa = ex.particles();
+        size_t na = ex.initialized() ? ex.n_alive_host() : pa.n;
+        std::vector<size_t> order(na);
+        for (size_t k = 0; k < na; k++) order[k] = k;
+        std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return pa.id[a] < pa.id[b]; });
+        const glisser::Planets& pl = ex.initialized() ? ex.planets_snapshot() : ex.planets_live();
+        glisser::write_track(out, pl, pa, order, ex.t, ex.cfg.write_bary_track);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_write_plhist(const glisser_t* h, const char* path, int begin)
+{
+    glisser_t* hh = const_cast<glisser_t*>(h);
+    return guarded(hh, [&] {
+        glisser::Executor& ex = exec_of(hh);
+        std::ofstream out(path, begin ? std::ios::binary : (std::ios::binary | std::ios::app));
+        if (!out) throw glisser::IoError(std::string("cannot write ") + path);
+        const glisser::Planets& pl = ex.initialized() ? ex.planets_snapshot() : ex.planets_live();
+        if (begin) glisser::write_plhist_header(out, pl);
+        glisser::write_plhist_record(out, pl, ex.t);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_from_elements_M(double mu, double a, double e, double i, double capom, double om, double M, double* r3,
+                            double* v3)
+{
+    if (!r3 || !v3) return GLISSER_E_INVALID;
+    glisser::Vec3 r, v;
+    glisser::from_elements_M(mu, a, e, i, capom, om, M, r, v);
+    r3[0] = r.x; r3[1] = r.y; r3[2] = r.z;
+    v3[0] = v.x; v3[1] = v.y; v3[2] = v.z;
+    return GLISSER_OK;
+}
+
+int glisser_stats(const glisser_t* h, unsigned long long* particle_steps, unsigned long long* kepler_evals)
+{
+    if (!h) return GLISSER_E_INVALID;
+    if (particle_steps) *particle_steps = h->ex->particle_steps();
+    if (kepler_evals) *kepler_evals = h->ex->kepler_evals();
+    return GLISSER_OK;
+}
+
+int glisser_launches(const glisser_t* h, unsigned long long* launches)
+{
+    if (!h || !launches) return GLISSER_E_INVALID;
+    *launches = h->ex->launches();
+    return GLISSER_OK;
+}
+
+int glisser_stream(const glisser_t* h, void** stream)
+{
+    if (!h || !stream) return GLISSER_E_INVALID;
+    *stream = h->ex->stream();
+    return GLISSER_OK;
+}
+
+int glisser_elements_to_cartesian(size_t n, double mu, const double* el, double* r3, double* v3)
+{
+    if (n && (!el || !r3 || !v3)) return GLISSER_E_INVALID;
+    for (size_t k = 0; k < n; k++) {
+        glisser::Vec3 r, v;
+        const double* e = el + 6 * k;
+        glisser::from_elements_M(mu, e[0], e[1], e[2], e[3], e[4], e[5], r, v);
+        r3[3 * k] = r.x; r3[3 * k + 1] = r.y; r3[3 * k + 2] = r.z;
+        v3[3 * k] = v.x; v3[3 * k + 1] = v.y; v3[3 * k + 2] = v.z;
+    }
+    return GLISSER_OK;
+}
+
+int glisser_to_elements(double mu, const double* r3, const double* v3, int* esign, double* out6)
+{
+    if (!r3 || !v3 || !out6) return GLISSER_E_INVALID;
+    glisser::Elements el = glisser::to_elements(mu, { r3[0], r3[1], r3[2] }, { v3[0], v3[1], v3[2] });
+    if (esign) *esign = el.esign;
+    out6[0] = el.a; out6[1] = el.e; out6[2] = el.i; out6[3] = el.capom; out6[4] = el.om; out6[5] = el.f;
+    return GLISSER_OK;
+}
+
+}  // extern "C"

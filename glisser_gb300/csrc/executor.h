@@ -1,0 +1,106 @@
+// Block-loop executor: the GB300 replacement of sr::exec::Executor and
+// ExecutorFacade (src/executor.cu, src/executor_facade.{h,cu}).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <fstream>
+#include <memory>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/glisser.h"
+#include "config.h"
+#include "planets.h"
+#include "state_io.h"
+
+namespace glisser {
+
+struct CudaError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+struct FlaggedEntry {
+    uint32_t id;
+    uint16_t flags;
+    uint32_t deathtime_index;
+};
+
+class Executor {
+public:
+    explicit Executor(const Config& cfg);
+    ~Executor();
+    Executor(const Executor&) = delete;
+    Executor& operator=(const Executor&) = delete;
+
+    Config cfg;
+    std::string warnings;
+
+    void load();                                        // load_data
+    void set_planets(size_t n, const double* m, const double* r, const double* v, const uint32_t* id);
+    void set_particles(size_t n, const double* r, const double* v, const uint32_t* id, const uint16_t* flags,
+                       const double* deathtime);
+    void init();                                        // Executor::init
+    bool step_block(double* cpu_ms, double* gpu_ms);    // Executor::loop
+    void finish();                                      // Executor::finish
+
+    // host views (downloaded on demand)
+    const Particles& particles();
+    const Planets& planets_snapshot() const { return snapshot_; }
+    const Planets& planets_live() const { return pl_; }
+    const std::vector<FlaggedEntry>& last_flagged() const { return flagged_; }
+    // the planet block the next step_block integrates with
+    void planet_block(std::vector<double>& log, std::vector<double>& m, std::vector<uint32_t>& id,
+                      std::vector<double>& rh, uint32_t& npl, uint32_t& len) const;
+
+    double t = 0, e0 = 0;
+    size_t n_alive_host() const { return n_dev_ + n_encounter_; }
+    size_t n_encounter() const { return n_encounter_; }
+    size_t n_total() const { return pa_.n; }
+    bool initialized() const { return initialized_; }
+
+    // Kepler starter selection (GLISSER_STARTER_*) and learned weights blob
+    void set_starter(int starter, const std::vector<uint8_t>* mlp_blob);
+    unsigned long long kepler_evals() const { return evals_total_; }
+    unsigned long long particle_steps() const { return psteps_total_; }
+    unsigned long long launches() const { return launches_total_; }
+    void* stream() const;
+
+    std::ostream* log = nullptr;             // progress / warnings (stdout tee)
+    std::ostream* encounter_out = nullptr;   // encounter.out
+
+private:
+    Planets pl_;            // live planets (one block ahead of the particles after init)
+    Planets snapshot_;      // planets at the particles' time
+    Particles pa_;          // host mirror in device order
+    std::unordered_map<uint32_t, double> deathtime_;
+    bool loaded_pl_ = false, loaded_pa_ = false, initialized_ = false, host_dirty_ = false;
+
+    PlanetIntegrator integ_;
+    HistoryInterpolator interp_;
+    std::vector<double> rh_;
+    double cur_dt_ = 0, prev_dt_ = 0;
+    size_t cur_tbsize_ = 0, prev_tbsize_ = 0;
+    bool starting_interval_ = false;
+    int starter_ = GLISSER_STARTER_SERIES;
+    unsigned long long evals_total_ = 0;
+    unsigned long long psteps_total_ = 0;
+    unsigned long long launches_total_ = 0;
+
+    size_t n_dev_ = 0, n_encounter_ = 0;
+    std::vector<FlaggedEntry> flagged_;
+
+    struct Impl;
+    std::unique_ptr<Impl> d_;
+
+    void update_planets();
+    void initial_accelerations(std::vector<Vec3>& acc);
+    void upload_particles(const std::vector<Vec3>& acc);
+    void download_particles();
+};
+
+// targets/main.cpp as a library call: runs to Final-Time writing the standard
+// output folder.  Returns 0, or -1 after writing the end state on an error.
+int run_main(Executor& ex, bool quiet, bool force, std::string& error);
+
+}  // namespace glisser

@@ -1,0 +1,287 @@
+// Universal-variable Kepler drift for the particle time-block kernel.
+//
+// Solves  f(s) = r0*G1(s) + u*G2(s) + mu*G3(s) - dt = 0  for the universal
+// anomaly s, with G_k(s) = s^k c_k(alpha s^2) the Stumpff-scaled G-functions
+// (Danby, Fundamentals of Celestial Mechanics, sec. 6.9; the reference's
+// spec is kepu, src/wh.cpp:131-420, itself SWIFT's drift_kepu*), then applies
+// the f and g functions (src/wh.cpp:843-851).
+//
+// The arithmetic is FP64 throughout.  GB300 issues FP64 at a small fraction
+// of its FP32 rate, so the solver is written to minimise FP64 instructions:
+//  * one reciprocal per Newton pass: the quartic correction is the series
+//    reversion  ds = -h - A h^2 + (B - 2A^2) h^3  (h = f/f', A = f''/2f',
+//    B = f'''/6f'), which has the same fourth-order convergence as the
+//    reference's three nested divisions;
+//  * convergence is judged on the residual at the current s, |f| < tol*dt
+//    (the reference's DANBYB test); the quartic correction computed in that
+//    same pass is then folded into the G-functions by Taylor expansion
+//    (dG3 = G2 ds, dG2 = G1 ds, dG1 = G0 ds, dG0 = -alpha G1 ds), so the
+//    accepted solution carries an O(tol^4) error instead of O(tol) and no
+//    second Stumpff evaluation is needed for it;
+//  * the Stumpff series is evaluated by Horner in x = alpha s^2; arguments
+//    with |x| >= 0.1 are quartered and rebuilt with the double-angle
+//    identities (c0,c1,c2,c3 as in Danby eq. 6.9.15).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "mlp.cuh"
+
+namespace glisser {
+
+constexpr double KEP_TOL = 1e-13;       // |f|/dt acceptance (reference DANBYB)
+constexpr int KEP_NEWTON_MAX = 8;       // quartic passes before Laguerre
+constexpr int KEP_LAGUERRE_MAX = 200;   // bounded fallback passes
+
+enum Starter : int {
+    STARTER_CLASSIC = 0,   // the reference's kepu_guess (src/wh.cpp:188-220)
+    STARTER_SERIES = 1,    // third-order time series, else FP32 Kepler pre-solve
+    STARTER_LEARNED = 2,   // MLP over drift invariants, series fallback
+};
+
+struct GFun {
+    double g0, g1, g2, g3;
+};
+
+// Stumpff c2(x), c3(x) series coefficients: (-1)^k/(2k+2)! and (-1)^k/(2k+3)!
+__device__ __forceinline__ void stumpff_small(double x, double& c2, double& c3)
+{
+    c2 = fma(x, 1.0 / 87178291200.0, -1.0 / 479001600.0);
+    c2 = fma(x, c2, 1.0 / 3628800.0);
+    c2 = fma(x, c2, -1.0 / 40320.0);
+    c2 = fma(x, c2, 1.0 / 720.0);
+    c2 = fma(x, c2, -1.0 / 24.0);
+    c2 = fma(x, c2, 0.5);
+    c3 = fma(x, 1.0 / 1307674368000.0, -1.0 / 6227020800.0);
+    c3 = fma(x, c3, 1.0 / 39916800.0);
+    c3 = fma(x, c3, -1.0 / 362880.0);
+    c3 = fma(x, c3, 1.0 / 5040.0);
+    c3 = fma(x, c3, -1.0 / 120.0);
+    c3 = fma(x, c3, 1.0 / 6.0);
+}
+
+__device__ __forceinline__ GFun gfuns(double s, double alpha)
+{
+    double s2 = s * s;
+    double x = alpha * s2;
+    double c0, c1, c2, c3;
+    if (fabs(x) < 0.1) {
+        stumpff_small(x, c2, c3);
+        c1 = fma(-x, c3, 1.0);
+        c0 = fma(-x, c2, 1.0);
+    } else {
+        // quarter the argument until |x| < 0.1, then rebuild (bounded: x
+        // finite needs at most ~520 quarterings; non-finite x stops at 600)
+        int n = 0;
+        while (fabs(x) >= 0.1 && n < 600) {
+            x *= 0.25;
+            n++;
+        }
+        stumpff_small(x, c2, c3);
+        c1 = fma(-x, c3, 1.0);
+        c0 = fma(-x, c2, 1.0);
+        for (int i = 0; i < n; i++) {
+            c3 = (c2 + c0 * c3) * 0.25;
+            c2 = c1 * c1 * 0.5;
+            c1 = c0 * c1;
+            c0 = fma(2.0 * c0, c0, -1.0);
+        }
+    }
+    GFun g;
+    g.g0 = c0;
+    g.g1 = s * c1;
+    g.g2 = s2 * c2;
+    g.g3 = s2 * s * c3;
+    return g;
+}
+
+// Real root of the cubic truncation of Kepler's equation (src/wh.cpp:131-173);
+// returns false when there is none.
+__device__ __forceinline__ bool p3solve(double dt, double r0, double mu, double alpha, double u, double& s)
+{
+    double denom = (mu - alpha * r0) / 6.0;
+    double a2 = 0.5 * u / denom;
+    double a1 = r0 / denom;
+    double a0 = -dt / denom;
+    double q = (a1 - a2 * a2 / 3.0) / 3.0;
+    double r = (a1 * a2 - 3.0 * a0) / 6.0 - (a2 * a2 * a2) / 27.0;
+    double sq2 = q * q * q + r * r;
+    if (!(sq2 >= 0)) return false;
+    double sq = sqrt(sq2);
+    double p1 = cbrt(r + sq);
+    double p2 = cbrt(r - sq);
+    s = p1 + p2 - a2 / 3.0;
+    return true;
+}
+
+// The reference's classic starter (src/wh.cpp:188-220, SWIFT drift_kepu_guess).
+__device__ __forceinline__ double starter_classic(double dt, double r0, double rinv, double mu, double alpha, double u)
+{
+    double s;
+    if (alpha > 0) {
+        if (dt * rinv <= 0.4) {
+            s = dt * rinv - (dt * dt * u) * 0.5 * rinv * rinv * rinv;
+        } else {
+            double a = mu / alpha;
+            double en = sqrt(mu / (a * a * a));
+            double ec = 1.0 - r0 / a;
+            double es = u / (en * a * a);
+            double e = sqrt(ec * ec + es * es);
+            double y = en * dt - es;
+            double sy, cy;
+            sincos(y, &sy, &cy);
+            double sigma = es * cy + ec * sy > 0 ? 1.0 : -1.0;
+            s = (y + sigma * 0.85 * e) * rsqrt(alpha);
+        }
+    } else {
+        if (!p3solve(dt, r0, mu, alpha, u, s)) s = dt * rinv;
+    }
+    return s;
+}
+
+// FP32 pre-solve of the elliptic Kepler equation in the difference form
+//   x - ec sin x + es (1 - cos x) = dM,   s = x / sqrt(alpha)
+// (ec = 1 - r0 alpha/mu, es = u sqrt(alpha)/mu).  Runs on the FP32 pipes; its
+// ~1e-6 relative accuracy only has to put the FP64 iteration in its
+// quartic basin.
+__device__ __forceinline__ double starter_fp32_kepler(double dt, double r0, double mu, double alpha, double u)
+{
+    double sa = sqrt(alpha);
+    double n = alpha * sa / mu;                       // mean motion
+    const double two_pi = 6.283185307179586;
+    double dM = n * dt;
+    double turns = floor(dM / two_pi);
+    float dMf = (float)(dM - turns * two_pi);
+    float ec = (float)(1.0 - r0 * alpha / mu);
+    float es = (float)(u * sa / mu);
+    // Danby's starter for the difference equation
+    float sM, cM;
+    __sincosf(dMf, &sM, &cM);
+    float x = dMf - es + es * cM + ec * sM;
+    for (int k = 0; k < 6; k++) {
+        float sx, cx;
+        sincosf(x, &sx, &cx);
+        float f = x - ec * sx + es * (1.0f - cx) - dMf;
+        float fp = 1.0f - ec * cx + es * sx;
+        float fpp = ec * sx + es * cx;
+        float dx = -f / fp;
+        dx = -f / (fp + 0.5f * dx * fpp);
+        x += dx;
+    }
+    return ((double)x + turns * two_pi) / sa;
+}
+
+// Third-order expansion of s(dt) about s = 0:
+//   s = t/r0 - u t^2/(2 r0^3) + (u^2/(2 r0^5) - (mu - alpha r0)/(6 r0^4)) t^3
+__device__ __forceinline__ double starter_series3(double dt, double rinv, double mu, double alpha, double u, double r0)
+{
+    double tau = dt * rinv;                  // dt / r0
+    double k = mu - alpha * r0;
+    double c2 = -0.5 * u * rinv;             // coefficient of tau^2
+    double c3 = fma(0.5 * u * rinv, u * rinv, -k * rinv * (1.0 / 6.0));
+    return tau * fma(tau, fma(tau, c3, c2), 1.0);
+}
+
+struct DriftResult {
+    uint16_t flags;     // 0x08 unbound, 0x04 not converged
+    uint16_t evals;     // Stumpff evaluations spent
+};
+
+// Drifts (r, v) by dt about a central mass mu.
+__device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, double& rz, double& vx, double& vy, double& vz,
+                                                   double dt, double mu, int starter, const MlpDev* mlp)
+{
+    double r2 = fma(rx, rx, fma(ry, ry, rz * rz));
+    double v2 = fma(vx, vx, fma(vy, vy, vz * vz));
+    double u = fma(rx, vx, fma(ry, vy, rz * vz));
+    double rinv = rsqrt(r2);
+    double r0 = r2 * rinv;
+    double mu_r = mu * rinv;
+    double alpha = fma(2.0, mu_r, -v2);
+    DriftResult res;
+    res.flags = alpha <= 0 ? 0x08 : 0;
+    res.evals = 0;
+
+    double s;
+    double tau_dyn = dt * rinv * sqrt(mu_r);          // dt / (r0 / v_circ): dimensionless step
+    if (starter == STARTER_CLASSIC) {
+        s = starter_classic(dt, r0, rinv, mu, alpha, u);
+    } else {
+        s = -1.0;
+        if (starter == STARTER_LEARNED && mlp) s = starter_learned(mlp, dt, r0, rinv, mu, alpha, u);
+        if (!(s > 0)) {
+            if (tau_dyn < 0.05) s = starter_series3(dt, rinv, mu, alpha, u, r0);
+            else if (alpha > 0) s = starter_fp32_kepler(dt, r0, mu, alpha, u);
+            else s = starter_classic(dt, r0, rinv, mu, alpha, u);
+        }
+    }
+
+    const double k = mu - alpha * r0;
+    const double ua = u * alpha;
+    const double tol = KEP_TOL * dt;
+    GFun g;
+    double fp = 0, fpp = 0, ds = 0, inv_fp = 0;
+    bool ok = false;
+    for (int it = 0; it < KEP_NEWTON_MAX; it++) {
+        g = gfuns(s, alpha);
+        res.evals++;
+        double f = fma(r0, g.g1, fma(u, g.g2, fma(mu, g.g3, -dt)));
+        fp = fma(r0, g.g0, fma(u, g.g1, mu * g.g2));
+        fpp = fma(k, g.g1, u * g.g0);
+        double fppp = fma(k, g.g0, -ua * g.g1);
+        inv_fp = 1.0 / fp;
+        double h = f * inv_fp;
+        double q = fpp * inv_fp;                      // 2A
+        double p = fppp * inv_fp;                     // 6B
+        // ds = -h (1 + A h - (B - 2A^2) h^2)
+        double corr = fma(h, fma(-h, fma(p, 1.0 / 6.0, -0.5 * q * q), 0.5 * q), 1.0);
+        ds = -h * corr;
+        if (fabs(f) < tol) {
+            ok = true;
+            break;
+        }
+        s += ds;
+    }
+    if (!ok) {
+        // Laguerre's method (n = 5) from the last iterate (SWIFT
+        // drift_kepu_lag, with the exact f'' = (mu - alpha r0) G1 + u G0)
+        const double ln = 5.0;
+        for (int it = 0; it < KEP_LAGUERRE_MAX; it++) {
+            g = gfuns(s, alpha);
+            res.evals++;
+            double f = fma(r0, g.g1, fma(u, g.g2, fma(mu, g.g3, -dt)));
+            fp = fma(r0, g.g0, fma(u, g.g1, mu * g.g2));
+            fpp = fma(k, g.g1, u * g.g0);
+            inv_fp = 1.0 / fp;
+            if (fabs(f) < tol) {
+                ds = -f * inv_fp;
+                ok = true;
+                break;
+            }
+            double disc = sqrt(fabs((ln - 1.0) * (ln - 1.0) * fp * fp - (ln - 1.0) * ln * f * fpp));
+            s = s - ln * f / (fp + (fp > 0 ? disc : -disc));
+        }
+        if (!ok) {
+            res.flags |= 0x04;
+            ds = 0;
+        }
+    }
+    // fold the last correction into the G-functions (Taylor in ds)
+    double hd = 0.5 * ds;
+    double g3 = fma(ds, fma(hd, g.g1, g.g2), g.g3);
+    double g2 = fma(ds, fma(hd, g.g0, g.g1), g.g2);
+    double g1 = fma(ds, fma(-hd * alpha, g.g1, g.g0), g.g1);
+    double rnew_inv = inv_fp * fma(-fpp * ds, inv_fp, 1.0);    // 1/f'(s+ds)
+
+    double ff = fma(-mu_r, g2, 1.0);
+    double gg = fma(-mu, g3, dt);
+    double fd = -mu_r * g1 * rnew_inv;
+    double gd = fma(-mu * g2, rnew_inv, 1.0);
+    double nrx = fma(ff, rx, gg * vx), nry = fma(ff, ry, gg * vy), nrz = fma(ff, rz, gg * vz);
+    double nvx = fma(fd, rx, gd * vx), nvy = fma(fd, ry, gd * vy), nvz = fma(fd, rz, gd * vz);
+    rx = nrx; ry = nry; rz = nrz;
+    vx = nvx; vy = nvy; vz = nvz;
+    return res;
+}
+
+}  // namespace glisser

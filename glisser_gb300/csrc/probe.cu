@@ -1,0 +1,62 @@
+// FP64 throughput probe: the denominator of the particle kernel's roofline.
+//
+// GB300's FP64 rate is a small fraction of its FP32 rate and the driver's
+// measured-peaks file has no FP64 entry, so the library measures it: every
+// thread runs 8 independent dependent chains of DFMA (enough to cover the
+// pipe latency), on a grid of 4 CTAs x 256 threads per SM, timed with CUDA
+// events.  2 flops per DFMA.
+#include <cuda_runtime.h>
+
+#include "../../include/glisser.h"
+
+namespace glisser {
+
+namespace {
+
+__global__ void __launch_bounds__(256) dfma_chains(double* out, int iters, double a, double b)
+{
+    double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+    double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    for (int k = 0; k < iters; k++) {
+#pragma unroll
+        for (int u = 0; u < 16; u++) {
+            x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+            x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+        }
+    }
+    double s = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+    if (s == 12345.678) out[0] = s;   // keeps the chains live; never true in practice
+}
+
+}  // namespace
+
+}  // namespace glisser
+
+extern "C" int glisser_fp64_peak_probe(double* tflops, double* ms)
+{
+    if (!tflops) return GLISSER_E_INVALID;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return GLISSER_E_CUDA;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return GLISSER_E_CUDA;
+    double* out = nullptr;
+    if (cudaMalloc(&out, sizeof(double)) != cudaSuccess) return GLISSER_E_CUDA;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    const int blocks = sms * 4, threads = 256, iters = 2048;
+    glisser::dfma_chains<<<blocks, threads>>>(out, 64, 0.999999, 1e-7);   // warm-up
+    cudaEventRecord(a);
+    glisser::dfma_chains<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+    cudaEventRecord(b);
+    cudaError_t e = cudaEventSynchronize(b);
+    float t = 0;
+    cudaEventElapsedTime(&t, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(out);
+    if (e != cudaSuccess || t <= 0) return GLISSER_E_CUDA;
+    double flops = 2.0 * 8 * 16 * (double)iters * blocks * threads;
+    *tflops = flops / (t * 1e-3) / 1e12;
+    if (ms) *ms = t;
+    return GLISSER_OK;
+}

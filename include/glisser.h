@@ -1,0 +1,224 @@
+/*
+ * glisser-gb300 C ABI.
+ *
+ * A drop-in for the massless-particle WH/MVS time-block path of glisser
+ * (skkestrel/glisser).  Every entry point returns an int status: 0 on
+ * success, a negative GLISSER_E_* code on failure, with the message available
+ * from glisser_last_error (handle-level calls) or glisser_last_error_global
+ * (handle-free calls).  No C++ exception crosses this boundary.  One host
+ * thread per handle.  The caller owns every host buffer it passes; the library
+ * owns the device buffers behind a handle.
+ *
+ * Two layers:
+ *   - the executor layer (glisser_create ... glisser_destroy) mirrors
+ *     sr::exec::ExecutorFacade (src/executor_facade.h:18-39) and the
+ *     Configuration / state / track / history formats of src/data.cpp;
+ *   - the kernel layer (glisser_integrate_timeblock and friends) mirrors the
+ *     device seam WHCudaIntegrator::integrate_particles_timeblock_cuda
+ *     (src/wh.cuh:51-57) for callers that manage device memory themselves.
+ */
+#ifndef GLISSER_H
+#define GLISSER_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GLISSER_OK 0
+#define GLISSER_E_INVALID -1   /* bad argument or call order */
+#define GLISSER_E_CONFIG -2    /* configuration text rejected (src/data.cpp:195-333) */
+#define GLISSER_E_IO -3        /* file missing, unreadable or unwritable */
+#define GLISSER_E_CUDA -4      /* a CUDA call failed (message names it) */
+#define GLISSER_E_STATE -5     /* simulation state invalid (unbound or unconverged planet) */
+#define GLISSER_E_NOMEM -6     /* allocation failed */
+#define GLISSER_E_EOS -7       /* planetary history ended (src/interp.h:64-68 EOSError) */
+#define GLISSER_E_RUNTIME -8   /* other runtime error (reference: std::runtime_error) */
+#define GLISSER_E_TIMEOUT -9   /* a bounded device wait gave up; the device status word says where */
+
+/* Particle flag bits (src/data.h:169-182).  High byte: planet id of an
+ * encounter or absorption. */
+#define GLISSER_FLAG_ENCOUNTER 0x0001
+#define GLISSER_FLAG_OUT_OF_BOUNDS 0x0002
+#define GLISSER_FLAG_KEPLER 0x0004
+#define GLISSER_FLAG_UNBOUND 0x0008
+#define GLISSER_FLAG_DEAD 0x0080
+
+/* Kepler starters for the universal-variable drift. */
+#define GLISSER_STARTER_CLASSIC 0  /* the reference's kepu_guess, src/wh.cpp:188-220 */
+#define GLISSER_STARTER_SERIES 1   /* third-order time series / FP32 Kepler pre-solve */
+#define GLISSER_STARTER_LEARNED 2  /* MLP initial guess, series fallback */
+
+/* ------------------------------------------------------------------------
+ * Kernel layer.  All pointers in these structs are DEVICE pointers.
+ * ---------------------------------------------------------------------- */
+
+/* Structure-of-arrays particle state (src/data.cuh:8-36 holds the same
+ * fields as AoS f64_3 plus the acceleration kept by WHCudaIntegrator). */
+typedef struct glisser_particles {
+    double *rx, *ry, *rz;        /* heliocentric position */
+    double *vx, *vy, *vz;        /* heliocentric velocity */
+    double *ax, *ay, *az;        /* acceleration carried to the next block */
+    uint16_t *flags;             /* deathflags */
+    uint32_t *deathtime_index;   /* last integrated step + 1 within the block */
+    uint32_t *id;
+} glisser_particles;
+
+/* One block of planet data (DevicePlanetPhaseSpace r_log plus the h0 log of
+ * WHCudaIntegrator, src/data.cuh:38-57, src/wh.cuh:17-20).  `log` holds, per
+ * step, a record of (npl) 3-vectors: h0 first, then the heliocentric
+ * positions of planets 1..npl-1.  `capacity` (records) must be at least
+ * len rounded up to even, and the buffer 16-byte aligned. */
+typedef struct glisser_planet_block {
+    const double *log;
+    const double *m;             /* [npl] G*mass; m[0] is the central mass mu */
+    const uint32_t *id;          /* [npl] planet ids (encounter flag high byte) */
+    const double *rh;            /* [npl] encounter radii; rh[0] is the Sun's cull radius */
+    uint32_t npl;                /* planets including the Sun, 1..64 */
+    uint32_t len;                /* steps in this block */
+    uint32_t capacity;
+    uint32_t reserved;
+} glisser_planet_block;
+
+typedef struct glisser_step_params {
+    double dt;
+    double outer_radius;         /* Outer-Limit */
+    int32_t starter;             /* GLISSER_STARTER_* */
+    int32_t kill_encounters;     /* nonzero: 0x01 -> 0x80 at block end (KillEncounterKernel) */
+    const void *mlp;             /* learned-starter weights (device), or NULL */
+} glisser_step_params;
+
+/* Hand-off of the particles flagged during a block, compacted by warp ballot
+ * (the encounter hand-off of src/executor.cu:470-596 consumes this list).
+ * `count` must be zeroed by the caller before the launch; on return it holds
+ * the number of newly flagged particles (entries beyond `capacity` are
+ * counted but not written).  `status` is ORed with GLISSER_STATUS_* bits.
+ * `evals` (optional) accumulates the Stumpff evaluations spent. */
+typedef struct glisser_handoff {
+    uint32_t *count;
+    uint32_t *index;             /* position in the particle arrays */
+    uint32_t *id;
+    uint16_t *flags;
+    uint32_t *deathtime_index;
+    uint32_t capacity;
+    uint32_t reserved;
+    uint32_t *status;
+    unsigned long long *evals;
+} glisser_handoff;
+
+#define GLISSER_STATUS_LOG_TIMEOUT 0x1u   /* planet-log staging wait gave up */
+
+/* Replaces WHCudaIntegrator::integrate_particles_timeblock_cuda
+ * (src/wh.cu:344-395): integrates particles [0, n_alive) over the block's
+ * len steps on `stream` (a cudaStream_t, NULL for the legacy stream).
+ * Asynchronous; errors in arguments return immediately. */
+int glisser_integrate_timeblock(const glisser_particles *pa, size_t n_alive, const glisser_planet_block *pl,
+                                const glisser_step_params *sp, const glisser_handoff *ho, void *stream);
+
+/* Stable three-way partition of particles [0, n): unflagged first, then
+ * encounter particles ((flags & 0xFE) == 0), then the rest -- the three
+ * thrust::partition calls of src/executor.cu:663-665, 784-790, made stable.
+ * `out` is a second particle buffer of the same capacity receiving the
+ * result; `scratch` is device memory of glisser_partition_scratch_bytes(n)
+ * bytes; n_unflagged / n_encounter (device, uint32) receive the counts. */
+size_t glisser_partition_scratch_bytes(size_t n);
+int glisser_partition(const glisser_particles *in, const glisser_particles *out, size_t n, void *scratch,
+                      uint32_t *n_unflagged, uint32_t *n_encounter, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Executor layer (host buffers).
+ * ---------------------------------------------------------------------- */
+
+typedef struct glisser_s glisser_t;
+
+/* Parses a configuration text with the reference's keys, defaults and
+ * validation (read_configuration, src/data.cpp:146-333). */
+int glisser_create(const char *config_text, glisser_t **out);
+int glisser_destroy(glisser_t *h);
+int glisser_last_error(const glisser_t *h, char *buf, size_t cap);
+int glisser_last_error_global(char *buf, size_t cap);
+
+/* Reads a configuration value back by its key (as text). */
+int glisser_config_get(const glisser_t *h, const char *key, char *buf, size_t cap);
+/* Writes the configuration as write_configuration does (src/data.cpp:335-372). */
+int glisser_write_config(const glisser_t *h, const char *path, double t0, double tf);
+
+/* load_data (src/data.cpp:527-584): the Input-File (ASCII or binary per
+ * Read-Binary-Input) or the split Planet/Particle-Input-File pair. */
+int glisser_load_state(glisser_t *h);
+/* Or hand the state over from memory: vectors are [n][3]. */
+int glisser_set_planets(glisser_t *h, size_t n, const double *m, const double *r, const double *v, const uint32_t *id);
+int glisser_set_particles(glisser_t *h, size_t n, const double *r, const double *v, const uint32_t *id,
+                          const uint16_t *flags, const double *deathtime);
+
+/* Executor::init (src/executor.cu:85-217). */
+int glisser_init(glisser_t *h);
+/* Executor::loop (src/executor.cu:598-764): one time block.  *safe_to_output
+ * mirrors loop's return value. */
+int glisser_step_block(glisser_t *h, int *safe_to_output, double *cpu_ms, double *gpu_ms);
+/* Runs blocks until Final-Time, writing the outputs main() writes
+ * (targets/main.cpp:146-356) under Output-Folder. */
+int glisser_run(glisser_t *h, int quiet);
+/* Executor::finish (src/executor.cu:880-890). */
+int glisser_finish(glisser_t *h);
+
+int glisser_time(const glisser_t *h, double *t);
+int glisser_energy0(const glisser_t *h, double *e0);
+int glisser_counts(const glisser_t *h, size_t *n, size_t *n_alive, size_t *n_encounter);
+
+/* Copies the host mirror of the particles (refreshed after every block).
+ * Arrays may be NULL to skip a field; *n receives the particle count. */
+int glisser_get_particles(const glisser_t *h, double *r, double *v, uint32_t *id, uint16_t *flags,
+                          double *deathtime, uint32_t *deathtime_index, size_t cap, size_t *n);
+/* Planet snapshot at the particles' time (HostData::planets_snapshot). */
+int glisser_get_planets(const glisser_t *h, double *m, double *r, double *v, uint32_t *id, size_t cap, size_t *n);
+/* The planet block the next glisser_step_block integrates with: per step a
+ * record of npl 3-vectors (h0, then planets 1..npl-1), as uploaded to the
+ * device (WHCudaIntegrator's h0 log and DevicePlanetPhaseSpace::r_log,
+ * src/wh.cu:306-311, src/executor.cu:442-461).  `log` holds cap_steps
+ * records of 64 vectors at most; *npl and *len receive the block's shape. */
+int glisser_get_planet_block(const glisser_t *h, double *log, double *m, uint32_t *id, double *rh, uint32_t cap_steps,
+                             uint32_t *npl, uint32_t *len);
+/* The particles flagged in the last block (the compacted hand-off list). */
+int glisser_get_flagged(const glisser_t *h, uint32_t *ids, uint16_t *flags, uint32_t *deathtime_index,
+                        size_t cap, size_t *n);
+
+/* save_data (src/data.cpp:586-716), save_binary_track (src/data.cpp:718-815),
+ * begin/save_swift_plhist (src/data.cpp:817-877) on the current state. */
+int glisser_write_state(const glisser_t *h, const char *path, int binary);
+int glisser_write_track(const glisser_t *h, const char *path, int append);
+int glisser_write_plhist(const glisser_t *h, const char *path, int begin);
+
+/* Selects the Kepler starter (default GLISSER_STARTER_SERIES) and, for the
+ * learned starter, the weights blob written by glisser_mlp_save. */
+int glisser_set_starter(glisser_t *h, int starter, const char *mlp_path);
+
+/* Running totals since init: particle-steps integrated (each particle counts
+ * the steps it actually advanced, deathtime_index-aware) and Stumpff
+ * evaluations spent by the Kepler solver.  No reference counterpart; the
+ * reference reports timings only (timing.out, src/executor.cu:739-759). */
+int glisser_stats(const glisser_t *h, unsigned long long *particle_steps, unsigned long long *kepler_evals);
+/* Kernel launches issued by the executor since init, and its CUDA stream
+ * (a cudaStream_t; the blocks' kernels and copies run on it). */
+int glisser_launches(const glisser_t *h, unsigned long long *launches);
+int glisser_stream(const glisser_t *h, void **stream);
+
+/* Element conversions (src/convert.cpp:257-497). */
+int glisser_from_elements_M(double mu, double a, double e, double i, double capom, double om, double M,
+                            double *r3, double *v3);
+int glisser_to_elements(double mu, const double *r3, const double *v3, int *esign, double *out6);
+/* Batched from_elements_M over n element rows (a, e, i, capom, om, M): the
+ * particle generator of targets/make_state.cpp:126-165 without its RNG. */
+int glisser_elements_to_cartesian(size_t n, double mu, const double *el6, double *r3, double *v3);
+
+/* Measures this GPU's FP64 FMA throughput (TFLOP/s, 2 flops per DFMA) with a
+ * short probe kernel; *ms receives its duration.  No reference counterpart:
+ * it is the denominator of the particle kernel's roofline. */
+int glisser_fp64_peak_probe(double *tflops, double *ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1406,3 +1406,6 @@ int orc_planet_steps(size_t npl, const double* m, double* r, double* v, double d
 	planets_free(p);
 	return err;
 }
+
+/* Time step of the block the next orc_exec_loop integrates. */
+double orc_exec_dt(orc_exec* e) { return e->cur_dt; }

@@ -70,6 +70,8 @@ def lib():
         L.orc_exec_planets.argtypes = [C.c_void_p, C.POINTER(C.c_size_t), D, D, D, U32]
         L.orc_planet_steps.argtypes = [C.c_size_t, D, D, D, C.c_double, C.c_size_t, D, D, D]
         L.orc_planet_steps.restype = C.c_int
+        L.orc_exec_dt.argtypes = [C.c_void_p]
+        L.orc_exec_dt.restype = C.c_double
         _lib = L
     return _lib
 
@@ -160,7 +162,8 @@ class Exec:
         t = C.c_double()
         npl, ln = C.c_uint32(), C.c_uint32()
         lib().orc_exec_counts(self.h, C.byref(n), C.byref(na), C.byref(t), C.byref(npl), C.byref(ln))
-        return dict(n=n.value, n_alive=na.value, t=t.value, npl=npl.value, log_len=ln.value)
+        return dict(n=n.value, n_alive=na.value, t=t.value, npl=npl.value, log_len=ln.value,
+                    dt=lib().orc_exec_dt(self.h))
 
     def particles(self):
         n = self.counts()["n"]
