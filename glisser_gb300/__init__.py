@@ -13,7 +13,7 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "libglisser_gb300.so")
+LIB_PATH = os.path.join(os.environ.get("GLISSER_BUILD_DIR") or os.path.join(HERE, "_build"), "libglisser_gb300.so")
 
 OK = 0
 E_INVALID, E_CONFIG, E_IO, E_CUDA, E_STATE, E_NOMEM, E_EOS, E_RUNTIME, E_TIMEOUT = range(-1, -10, -1)
@@ -115,6 +115,7 @@ def lib():
             "glisser_elements_to_cartesian": ([C.c_size_t, C.c_double, D, D, D], C.c_int),
             "glisser_fp64_peak_probe": ([D, D], C.c_int),
             "glisser_launches": ([P, C.POINTER(C.c_ulonglong)], C.c_int),
+            "glisser_l2_flush": ([P, C.c_size_t], C.c_int),
             "glisser_stream": ([P, C.POINTER(P)], C.c_int),
         }
         for name, (args, res) in sig.items():
@@ -168,6 +169,13 @@ def fp64_peak_probe():
     if rc:
         _raise(rc, last_error())
     return tf.value, ms.value
+
+
+def l2_flush(stream, nbytes=256 << 20):
+    """Overwrites nbytes of device scratch on `stream` (cold L2 for the next kernel)."""
+    rc = lib().glisser_l2_flush(C.c_void_p(stream), nbytes)
+    if rc:
+        _raise(rc, last_error())
 
 
 def to_elements(mu, r, v):

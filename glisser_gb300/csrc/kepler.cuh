@@ -13,11 +13,17 @@
 //    B = f'''/6f'), which has the same fourth-order convergence as the
 //    reference's three nested divisions;
 //  * convergence is judged on the residual at the current s, |f| < tol*dt
-//    (the reference's DANBYB test); the quartic correction computed in that
+//    (the reference's DANBYB test); the Newton correction computed in that
 //    same pass is then folded into the G-functions by Taylor expansion
-//    (dG3 = G2 ds, dG2 = G1 ds, dG1 = G0 ds, dG0 = -alpha G1 ds), so the
-//    accepted solution carries an O(tol^4) error instead of O(tol) and no
-//    second Stumpff evaluation is needed for it;
+//    (dG3 = G2 ds, dG2 = G1 ds, dG1 = G0 ds), so the accepted solution
+//    carries an O(tol^2) error instead of O(tol) and no second Stumpff
+//    evaluation is needed for it;
+//  * the default starter is a seventh-order reversion of the time series of
+//    Kepler's equation, accurate to ~1e-16 for steps well inside an orbit,
+//    so the residual test normally accepts it on the first evaluation: one
+//    Stumpff evaluation per drift;
+//  * threshold tests on non-negative values compare the IEEE bit patterns as
+//    integers (same answer, including NaN, but on the integer pipe);
 //  * the Stumpff series is evaluated by Horner in x = alpha s^2; arguments
 //    with |x| >= 0.1 are quartered and rebuilt with the double-angle
 //    identities (c0,c1,c2,c3 as in Danby eq. 6.9.15).
@@ -25,6 +31,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "fastmath.cuh"
 #include "mlp.cuh"
 
 namespace glisser {
@@ -35,7 +42,7 @@ constexpr int KEP_LAGUERRE_MAX = 200;   // bounded fallback passes
 
 enum Starter : int {
     STARTER_CLASSIC = 0,   // the reference's kepu_guess (src/wh.cpp:188-220)
-    STARTER_SERIES = 1,    // third-order time series, else FP32 Kepler pre-solve
+    STARTER_SERIES = 1,    // seventh-order time-series reversion, else FP32 Kepler pre-solve
     STARTER_LEARNED = 2,   // MLP over drift invariants, series fallback
 };
 
@@ -60,12 +67,26 @@ __device__ __forceinline__ void stumpff_small(double x, double& c2, double& c3)
     c3 = fma(x, c3, 1.0 / 6.0);
 }
 
+// c2, c3 to x^3 only: enough when |x| < 2e-3 (the x^4 terms are below
+// 2e-3^4 / 3628800 ~ 4e-18 of c2)
+__device__ __forceinline__ void stumpff_short(double x, double& c2, double& c3)
+{
+    c2 = fma(x, fma(x, fma(x, -1.0 / 40320.0, 1.0 / 720.0), -1.0 / 24.0), 0.5);
+    c3 = fma(x, fma(x, fma(x, -1.0 / 362880.0, 1.0 / 5040.0), -1.0 / 120.0), 1.0 / 6.0);
+}
+
 __device__ __forceinline__ GFun gfuns(double s, double alpha)
 {
     double s2 = s * s;
     double x = alpha * s2;
     double c0, c1, c2, c3;
-    if (fabs(x) < 0.1) {
+    bool small = lt_nonneg(fabs(x), 2e-3);
+    if (__all_sync(__activemask(), small)) {
+        // warp-uniform: every lane in this pass has a small argument
+        stumpff_short(x, c2, c3);
+        c1 = fma(-x, c3, 1.0);
+        c0 = fma(-x, c2, 1.0);
+    } else if (fabs(x) < 0.1) {
         stumpff_small(x, c2, c3);
         c1 = fma(-x, c3, 1.0);
         c0 = fma(-x, c2, 1.0);
@@ -182,19 +203,59 @@ __device__ __forceinline__ double starter_series3(double dt, double rinv, double
     return tau * fma(tau, fma(tau, c3, c2), 1.0);
 }
 
+// Seventh-order reversion of the time series of Kepler's equation.
+// With T = t/r0, t/r0 = s + c2 s^2 + ... + c6 s^6 where
+//   c2 = u/(2 r0), c3 = k/(6 r0), c4 = -alpha u/(24 r0), c5 = -alpha k/(120 r0),
+//   c6 = alpha^2 u/(720 r0)   (k = mu - alpha r0)
+// follows from the G-function series; its reversion (Abramowitz & Stegun
+// 3.6.25) in the dimensionless X = c2 T, Y = c3 T^2, Z = c4 T^3, W = c5 T^4,
+// V = c6 T^5 is
+//   s/T = 1 - X + (2X^2 - Y) + (-5X^3 + 5XY - Z)
+//           + (14X^4 - 21X^2 Y + 6XZ + 3Y^2 - W)
+//           + (-42X^5 + 84X^3 Y - 28X^2 Z - 28XY^2 + 7XW + 7YZ - V) + O7.
+// For steps well inside an orbit (|X|, sqrt|Y| ~ 1e-3) the neglected
+// eighth-order terms are ~1e-16, so the FP64 residual check usually accepts
+// this s on the first Stumpff evaluation.  Orders 2-4 are summed in FP64;
+// orders 5-7 (below 1e-9 of s) in FP32.
+__device__ __forceinline__ double starter_series6(double dt, double rinv, double alpha, double u, double k)
+{
+    double T = dt * rinv;
+    double T2 = T * T;
+    double X = 0.5 * (u * rinv) * T;
+    double Y = (k * rinv) * T2 * (1.0 / 6.0);
+    double A = alpha * T2;                        // Z = -A X / 12, W = -A Y / 20, V = A^2 X / 360
+    double Z = (-1.0 / 12.0) * A * X;
+    double low = fma(X, fma(X, fma(-5.0, X, 2.0), -1.0), fma(Y, fma(5.0, X, -1.0), -Z));
+    float x = __double2float_rn(X), y = __double2float_rn(Y), a = __double2float_rn(A);
+    float z = (-1.0f / 12.0f) * a * x;
+    float w = (-1.0f / 20.0f) * a * y;
+    float v = (1.0f / 360.0f) * a * a * x;
+    float x2 = x * x;
+    float o5 = fmaf(x2, fmaf(14.0f, x2, -21.0f * y), fmaf(6.0f * x, z, fmaf(3.0f * y, y, -w)));
+    float o6 = fmaf(x, fmaf(x2, fmaf(-42.0f, x2, 84.0f * y), fmaf(-28.0f * x, z, fmaf(-28.0f * y, y, 7.0f * w))),
+                    fmaf(7.0f * y, z, -v));
+    // seventh order (A&S 3.6.25 b7; c7 T^6 = A^2 Y / 840)
+    float x3 = x2 * x;
+    float o7 = 8.0f * (x * v + y * w) + 4.0f * z * z + 120.0f * x3 * z + 180.0f * x2 * y * y + 132.0f * x3 * x3 -
+               (1.0f / 840.0f) * a * a * y - 36.0f * x2 * w - 72.0f * x * y * z - 330.0f * x2 * x2 * y -
+               12.0f * y * y * y;
+    return fma(T, low + (double)(o5 + o6 + o7), T);
+}
+
 struct DriftResult {
     uint16_t flags;     // 0x08 unbound, 0x04 not converged
     uint16_t evals;     // Stumpff evaluations spent
 };
 
-// Drifts (r, v) by dt about a central mass mu.
+// Drifts (r, v) by dt about a central mass mu.  dt2mu = dt^2 mu (a per-
+// block constant: the step-size test compares tau^2 = dt^2 mu / r0^3).
 __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, double& rz, double& vx, double& vy, double& vz,
-                                                   double dt, double mu, int starter, const MlpDev* mlp)
+                                                   double r2, double dt, double mu, double dt2mu, int starter,
+                                                   const MlpDev* mlp)
 {
-    double r2 = fma(rx, rx, fma(ry, ry, rz * rz));
     double v2 = fma(vx, vx, fma(vy, vy, vz * vz));
     double u = fma(rx, vx, fma(ry, vy, rz * vz));
-    double rinv = rsqrt(r2);
+    double rinv = rsqrt_fast(r2);
     double r0 = r2 * rinv;
     double mu_r = mu * rinv;
     double alpha = fma(2.0, mu_r, -v2);
@@ -202,22 +263,21 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
     res.flags = alpha <= 0 ? 0x08 : 0;
     res.evals = 0;
 
+    const double k = fma(-alpha, r0, mu);
     double s;
-    double tau_dyn = dt * rinv * sqrt(mu_r);          // dt / (r0 / v_circ): dimensionless step
     if (starter == STARTER_CLASSIC) {
         s = starter_classic(dt, r0, rinv, mu, alpha, u);
     } else {
         s = -1.0;
         if (starter == STARTER_LEARNED && mlp) s = starter_learned(mlp, dt, r0, rinv, mu, alpha, u);
         if (!(s > 0)) {
-            if (tau_dyn < 0.05) s = starter_series3(dt, rinv, mu, alpha, u, r0);
+            double tau2 = dt2mu * (rinv * rinv) * rinv;     // (dt / dynamical time)^2
+            if (lt_nonneg(tau2, 0.0025)) s = starter_series6(dt, rinv, alpha, u, k);
             else if (alpha > 0) s = starter_fp32_kepler(dt, r0, mu, alpha, u);
             else s = starter_classic(dt, r0, rinv, mu, alpha, u);
         }
     }
 
-    const double k = mu - alpha * r0;
-    const double ua = u * alpha;
     const double tol = KEP_TOL * dt;
     GFun g;
     double fp = 0, fpp = 0, ds = 0, inv_fp = 0;
@@ -228,19 +288,20 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
         double f = fma(r0, g.g1, fma(u, g.g2, fma(mu, g.g3, -dt)));
         fp = fma(r0, g.g0, fma(u, g.g1, mu * g.g2));
         fpp = fma(k, g.g1, u * g.g0);
-        double fppp = fma(k, g.g0, -ua * g.g1);
-        inv_fp = 1.0 / fp;
+        inv_fp = rcp_fast(fp);
         double h = f * inv_fp;
-        double q = fpp * inv_fp;                      // 2A
-        double p = fppp * inv_fp;                     // 6B
-        // ds = -h (1 + A h - (B - 2A^2) h^2)
-        double corr = fma(h, fma(-h, fma(p, 1.0 / 6.0, -0.5 * q * q), 0.5 * q), 1.0);
-        ds = -h * corr;
-        if (fabs(f) < tol) {
+        if (lt_nonneg(fabs(f), tol)) {
+            // accepted: a Newton correction is exact to O(h^2) ~ 1e-26
+            ds = -h;
             ok = true;
             break;
         }
-        s += ds;
+        double fppp = fma(k, g.g0, -(u * alpha) * g.g1);
+        double q = fpp * inv_fp;                      // 2A
+        double p = fppp * inv_fp;                     // 6B
+        // quartic step: ds = -h (1 + A h - (B - 2A^2) h^2)
+        double corr = fma(h, fma(-h, fma(p, 1.0 / 6.0, -0.5 * q * q), 0.5 * q), 1.0);
+        s = fma(-h, corr, s);
     }
     if (!ok) {
         // Laguerre's method (n = 5) from the last iterate (SWIFT
@@ -266,11 +327,12 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
             ds = 0;
         }
     }
-    // fold the last correction into the G-functions (Taylor in ds)
-    double hd = 0.5 * ds;
-    double g3 = fma(ds, fma(hd, g.g1, g.g2), g.g3);
-    double g2 = fma(ds, fma(hd, g.g0, g.g1), g.g2);
-    double g1 = fma(ds, fma(-hd * alpha, g.g1, g.g0), g.g1);
+    // fold the last correction into the G-functions (dG3 = G2 ds, dG2 =
+    // G1 ds, dG1 = G0 ds; |ds| < 1e-13 s, so the second-order terms are
+    // below 1e-26)
+    double g3 = fma(ds, g.g2, g.g3);
+    double g2 = fma(ds, g.g1, g.g2);
+    double g1 = fma(ds, g.g0, g.g1);
     double rnew_inv = inv_fp * fma(-fpp * ds, inv_fp, 1.0);    // 1/f'(s+ds)
 
     double ff = fma(-mu_r, g2, 1.0);

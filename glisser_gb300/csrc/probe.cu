@@ -60,3 +60,21 @@ extern "C" int glisser_fp64_peak_probe(double* tflops, double* ms)
     if (ms) *ms = t;
     return GLISSER_OK;
 }
+
+// Writes `bytes` of a scratch buffer on `stream` so that the next kernel
+// starts with a cold L2 (benchmark hygiene).  The buffer is allocated on the
+// first call and kept for the process.
+extern "C" int glisser_l2_flush(void* stream, size_t bytes)
+{
+    static void* buf = nullptr;
+    static size_t cap = 0;
+    if (bytes > cap) {
+        if (buf) cudaFree(buf);
+        buf = nullptr;
+        cap = 0;
+        if (cudaMalloc(&buf, bytes) != cudaSuccess) return GLISSER_E_CUDA;
+        cap = bytes;
+    }
+    return cudaMemsetAsync(buf, (int)(bytes & 0xFF), bytes, (cudaStream_t)stream) == cudaSuccess ? GLISSER_OK
+                                                                                                 : GLISSER_E_CUDA;
+}

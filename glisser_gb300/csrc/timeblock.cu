@@ -112,16 +112,22 @@ __device__ __forceinline__ void planet_kick(const double* L, int j, double rx, d
     double dy = ry - L[3 * j + 1];
     double dz = rz - L[3 * j + 2];
     double rad = fma(dx, dx, fma(dy, dy, dz * dz));
-    if (rad < s_rh2[j] && flags == 0) flags = (uint16_t)((s_id[j] << 8) | 0x0001);
-    double inv = rsqrt(rad);
+    if (lt_nonneg(rad, s_rh2[j]) && flags == 0) flags = (uint16_t)((s_id[j] << 8) | 0x0001);
+    double inv = rsqrt_fast46(rad);
     double fac = s_m[j] * (inv * inv * inv);
     ax = fma(-dx, fac, ax);
     ay = fma(-dy, fac, ay);
     az = fma(-dz, fac, az);
 }
 
+// CTAs per SM the register allocation is sized for (FP64-pipe bound: more
+// resident warps only help cover FP64 latency)
+#ifndef GLISSER_TB_MIN_BLOCKS
+#define GLISSER_TB_MIN_BLOCKS 4
+#endif
+
 template <int NP>
-__global__ void __launch_bounds__(BLOCK_THREADS) timeblock_kernel(const KParams p)
+__global__ void __launch_bounds__(BLOCK_THREADS, GLISSER_TB_MIN_BLOCKS) timeblock_kernel(const KParams p)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ double s_m[MAX_PLANETS];
@@ -170,8 +176,20 @@ __global__ void __launch_bounds__(BLOCK_THREADS) timeblock_kernel(const KParams 
     uint32_t dti = 0;
     uint32_t evals = 0;
     const double hdt = p.dt * 0.5;
+    const double dt2mu = p.dt * p.dt * s_m[0];
     const double mu = s_m[0];
     const double rh2_sun = s_rh2[0];
+    // Kick-drift-kick with the two half kicks between consecutive steps
+    // merged into one full kick (v += a dt); a particle takes the closing half
+    // kick when it is flagged or the block ends, so its stored velocity is
+    // always at a step boundary.  |r|^2 from the Sun/outer test is the next
+    // drift's r0^2.
+    if (flags == 0 && p.len > 0) {
+        vx = fma(ax, hdt, vx);
+        vy = fma(ay, hdt, vy);
+        vz = fma(az, hdt, vz);
+    }
+    double r2 = fma(rx, rx, fma(ry, ry, rz * rz));
 
     for (uint32_t c = 0; c < nchunks; c++) {
         const uint32_t b = c & 1u;
@@ -189,10 +207,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) timeblock_kernel(const KParams 
         const uint32_t steps = min(p.chunk, p.len - first);
         for (uint32_t s = 0; s < steps; s++) {
             if (flags != 0) continue;
-            vx = fma(ax, hdt, vx);
-            vy = fma(ay, hdt, vy);
-            vz = fma(az, hdt, vz);
-            DriftResult d = kepler_drift(rx, ry, rz, vx, vy, vz, p.dt, mu, p.starter, p.mlp);
+            DriftResult d = kepler_drift(rx, ry, rz, vx, vy, vz, r2, p.dt, mu, dt2mu, p.starter, p.mlp);
             flags = d.flags;
             evals += d.evals;
             const double* L = L0 + (size_t)s * rec;
@@ -205,13 +220,14 @@ __global__ void __launch_bounds__(BLOCK_THREADS) timeblock_kernel(const KParams 
                 for (int j = 1; j <= np; j++)
                     planet_kick(L, j, rx, ry, rz, ax, ay, az, flags, s_m, s_rh2, s_id);
             }
-            double rad = fma(rx, rx, fma(ry, ry, rz * rz));
-            if (rad < rh2_sun) flags = 0x0001;
-            if (rad > p.outer2) flags = 0x0002;
-            vx = fma(ax, hdt, vx);
-            vy = fma(ay, hdt, vy);
-            vz = fma(az, hdt, vz);
+            r2 = fma(rx, rx, fma(ry, ry, rz * rz));
+            if (lt_nonneg(r2, rh2_sun)) flags = 0x0001;
+            if (gt_nonneg(r2, p.outer2)) flags = 0x0002;
             dti = first + s + 1;
+            const double kc = (flags != 0 || dti == p.len) ? hdt : p.dt;
+            vx = fma(ax, kc, vx);
+            vy = fma(ay, kc, vy);
+            vz = fma(az, kc, vz);
         }
         __syncthreads();
         if (tid == 0 && c + 2 < nchunks) {

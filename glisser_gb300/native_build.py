@@ -14,7 +14,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
-OUT = os.path.join(HERE, "_build")
+OUT = os.environ.get("GLISSER_BUILD_DIR") or os.path.join(HERE, "_build")
+EXTRA_NVCC = os.environ.get("GLISSER_NVCC_FLAGS", "").split()
 LIB = os.path.join(OUT, "libglisser_gb300.so")
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
@@ -46,7 +47,7 @@ def _compile(src, extra_flags=()):
     inc = ["-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
     if src.endswith(".cu"):
         cmd = [nvcc_path(), GENCODE, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
-               "-Xptxas", "-warn-spills", *inc, *extra_flags, "-c", src, "-o", obj + ".tmp"]
+               "-Xptxas", "-warn-spills", *inc, *EXTRA_NVCC, *extra_flags, "-c", src, "-o", obj + ".tmp"]
     else:
         cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra",
                "-I" + os.path.join(cuda_home(), "include"), *inc, "-c", src, "-o", obj + ".tmp"]

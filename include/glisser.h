@@ -217,6 +217,10 @@ int glisser_elements_to_cartesian(size_t n, double mu, const double *el6, double
  * short probe kernel; *ms receives its duration.  No reference counterpart:
  * it is the denominator of the particle kernel's roofline. */
 int glisser_fp64_peak_probe(double *tflops, double *ms);
+/* Overwrites `bytes` of a library-owned scratch buffer on `stream` (a
+ * cudaStream_t) so the next kernel starts with a cold L2; benchmark hygiene,
+ * no reference counterpart. */
+int glisser_l2_flush(void *stream, size_t bytes);
 
 #ifdef __cplusplus
 }
