@@ -117,6 +117,9 @@ def lib():
             "glisser_launches": ([P, C.POINTER(C.c_ulonglong)], C.c_int),
             "glisser_l2_flush": ([P, C.c_size_t], C.c_int),
             "glisser_stream": ([P, C.POINTER(P)], C.c_int),
+            "glisser_partition_noalloc_max_particles": ([], C.c_size_t),
+            "glisser_partition_noalloc": ([C.POINTER(ParticlesDev), C.POINTER(ParticlesDev), C.c_size_t, P, P, P],
+                                          C.c_int),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -343,3 +346,16 @@ def partition(src, dst, n, scratch, n0_ptr, n1_ptr, stream=0):
 
 def partition_scratch_bytes(n):
     return lib().glisser_partition_scratch_bytes(n)
+
+
+def partition_noalloc(src, dst, n, n0_ptr, n1_ptr, stream=0):
+    """glisser_partition without caller scratch and without any allocation
+    (see include/glisser.h for the size limit and sharing rules)."""
+    rc = lib().glisser_partition_noalloc(C.byref(src), C.byref(dst), n, C.c_void_p(n0_ptr), C.c_void_p(n1_ptr),
+                                         C.c_void_p(stream))
+    if rc:
+        _raise(rc, last_error())
+
+
+def partition_noalloc_max_particles():
+    return lib().glisser_partition_noalloc_max_particles()

@@ -21,6 +21,9 @@ size_t partition_scratch_bytes(size_t n);
 int launch_partition(const glisser_particles* in, const glisser_particles* out, size_t n, void* scratch,
                      uint32_t* n0, uint32_t* n1, cudaStream_t stream);
 size_t mlp_blob_bytes();
+size_t partition_noalloc_max_particles();
+int launch_partition_noalloc(const glisser_particles* in, const glisser_particles* out, size_t n, uint32_t* n0,
+                             uint32_t* n1, cudaStream_t stream);
 }  // namespace glisser
 
 struct glisser_s {
@@ -103,6 +106,23 @@ int glisser_partition(const glisser_particles* in, const glisser_particles* out,
 {
     int rc = glisser::launch_partition(in, out, n, scratch, n_unflagged, n_encounter, (cudaStream_t)stream);
     if (rc != GLISSER_OK) g_last_error = "glisser_partition failed";
+    return rc;
+}
+
+size_t glisser_partition_noalloc_max_particles(void) { return glisser::partition_noalloc_max_particles(); }
+
+int glisser_partition_noalloc(const glisser_particles* in, const glisser_particles* out, size_t n,
+                              uint32_t* n_unflagged, uint32_t* n_encounter, void* stream)
+{
+    if (n > glisser::partition_noalloc_max_particles()) {
+        g_last_error = "glisser_partition_noalloc: n = " + std::to_string(n) + " exceeds the built-in scratch limit of " +
+                       std::to_string(glisser::partition_noalloc_max_particles()) +
+                       " particles; use glisser_partition with caller-provided scratch";
+        return GLISSER_E_INVALID;
+    }
+    int rc = glisser::launch_partition_noalloc(in, out, n, n_unflagged, n_encounter, (cudaStream_t)stream);
+    if (rc == GLISSER_E_INVALID) g_last_error = "glisser_partition_noalloc: invalid argument";
+    else if (rc != GLISSER_OK) g_last_error = "glisser_partition_noalloc: CUDA call failed";
     return rc;
 }
 

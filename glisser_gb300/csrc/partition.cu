@@ -10,6 +10,7 @@
 // output buffer.  HBM traffic is one read of the flags plus one read and one
 // write of the 96-byte particle record.
 #include <cstdio>
+#include <mutex>
 
 #include "timeblock.cuh"
 
@@ -165,6 +166,76 @@ int launch_partition(const glisser_particles* in, const glisser_particles* out, 
     }
     uint32_t tiles = (uint32_t)((n + TILE - 1) / TILE);
     uint32_t* counts = reinterpret_cast<uint32_t*>(scratch);
+    count_kernel<<<tiles, TILE, 0, stream>>>(in->flags, (uint32_t)n, counts);
+    scan_kernel<<<1, SCAN_THREADS, 0, stream>>>(counts, tiles, n0, n1);
+    scatter_kernel<<<tiles, TILE, 0, stream>>>(*in, *out, (uint32_t)n, counts, n0, n1);
+    return cudaGetLastError() == cudaSuccess ? GLISSER_OK : GLISSER_E_CUDA;
+}
+
+
+// ---------------------------------------------------------------------------
+// Partition without allocation.
+//
+// For callers that must not allocate device memory at all: a host program
+// that runs inside another framework's memory pool or under a fixed device
+// budget, where a cudaMalloc would either be refused or would synchronise the
+// whole device and stall work the caller has in flight.  Such a caller still
+// owns the particle buffers and the two count words; the per-tile counts
+// that glisser_partition keeps in caller-provided scratch live here in a
+// file-scope device array instead.
+//
+// NOALLOC_MAX_PARTICLES bounds n: 2 counts per 256-particle tile, 256 KiB in
+// all, resident on every GPU that loads the library until the process exits.
+// Every call shares that array and leaves the last call's counts in it.  No
+// entry needs clearing before a call (count_kernel writes every tile's counts
+// before scan_kernel reads them), but two calls whose work overlaps on the
+// GPU, on one stream or several, race on the array and corrupt each other.
+constexpr size_t NOALLOC_MAX_PARTICLES = 8u << 20;
+constexpr size_t NOALLOC_TILES = NOALLOC_MAX_PARTICLES / TILE;
+
+static __device__ __align__(256) uint32_t g_noalloc_counts[2 * NOALLOC_TILES];
+
+namespace {
+
+// Device address of g_noalloc_counts per device.  In host code the array's
+// name is only a host-side stand-in; the address kernels need comes from
+// cudaGetSymbolAddress, resolved once per device with that device current.
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mutex;
+uint32_t* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+
+int noalloc_scratch(uint32_t** out)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES) return GLISSER_E_CUDA;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void* ptr = nullptr;
+        if (cudaGetSymbolAddress(&ptr, g_noalloc_counts) != cudaSuccess || !ptr) return GLISSER_E_CUDA;
+        g_noalloc_ptr[dev] = static_cast<uint32_t*>(ptr);
+    }
+    *out = g_noalloc_ptr[dev];
+    return GLISSER_OK;
+}
+
+}  // namespace
+
+size_t partition_noalloc_max_particles() { return NOALLOC_MAX_PARTICLES; }
+
+int launch_partition_noalloc(const glisser_particles* in, const glisser_particles* out, size_t n, uint32_t* n0,
+                             uint32_t* n1, cudaStream_t stream)
+{
+    if (!in || !out || !n0 || !n1) return GLISSER_E_INVALID;
+    if (n > NOALLOC_MAX_PARTICLES) return GLISSER_E_INVALID;
+    uint32_t* counts = nullptr;
+    int rc = noalloc_scratch(&counts);
+    if (rc != GLISSER_OK) return rc;
+    if (n == 0) {
+        cudaMemsetAsync(n0, 0, sizeof(uint32_t), stream);
+        cudaMemsetAsync(n1, 0, sizeof(uint32_t), stream);
+        return cudaGetLastError() == cudaSuccess ? GLISSER_OK : GLISSER_E_CUDA;
+    }
+    uint32_t tiles = (uint32_t)((n + TILE - 1) / TILE);
     count_kernel<<<tiles, TILE, 0, stream>>>(in->flags, (uint32_t)n, counts);
     scan_kernel<<<1, SCAN_THREADS, 0, stream>>>(counts, tiles, n0, n1);
     scatter_kernel<<<tiles, TILE, 0, stream>>>(*in, *out, (uint32_t)n, counts, n0, n1);

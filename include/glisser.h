@@ -127,6 +127,25 @@ size_t glisser_partition_scratch_bytes(size_t n);
 int glisser_partition(const glisser_particles *in, const glisser_particles *out, size_t n, void *scratch,
                       uint32_t *n_unflagged, uint32_t *n_encounter, void *stream);
 
+/* The same stable three-way partition for callers that cannot allocate
+ * device memory: for example a host program running inside another
+ * framework's memory pool or under a fixed device budget, where cudaMalloc is
+ * refused or would synchronise the device and stall its pipeline.  No
+ * counterpart in the reference.  It calls no cudaMalloc, cudaFree or other
+ * allocating routine: the per-tile scratch lives in a device array inside the
+ * library (256 KiB, resident on every GPU that loads the library until the
+ * process exits).  The caller still passes the particle buffers and the two
+ * count words.
+ *   - n may not exceed glisser_partition_noalloc_max_particles() (8,388,608);
+ *     larger n returns GLISSER_E_INVALID and launches nothing.
+ *   - The first call on a device looks up the array's device address; make
+ *     that first call before any stream capture.
+ *   - All calls share the array and leave their counts in it; calls whose
+ *     work overlaps on the GPU race and corrupt each other's result. */
+size_t glisser_partition_noalloc_max_particles(void);
+int glisser_partition_noalloc(const glisser_particles *in, const glisser_particles *out, size_t n,
+                              uint32_t *n_unflagged, uint32_t *n_encounter, void *stream);
+
 /* ------------------------------------------------------------------------
  * Executor layer (host buffers).
  * ---------------------------------------------------------------------- */
