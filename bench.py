@@ -173,6 +173,83 @@ def run_reference_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def ensemble_systems(G, fraction, rank, n_systems=256):
+    """Config 4 systems as (masses, planet r, planet v, particle r, particle v)."""
+    from glisser_gb300 import synth
+    out = []
+    for m, pel, el in synth.ensemble_workload(n_systems, seed=1000 * rank, fraction=fraction):
+        pr, pv = [np.zeros(3)], [np.zeros(3)]
+        for k in range(len(m) - 1):
+            a, b = G.elements_to_cartesian(m[0] + m[k + 1], pel[k:k + 1])
+            pr.append(a[0]); pv.append(b[0])
+        r, v = G.elements_to_cartesian(m[0], el)
+        out.append((m, np.array(pr), np.array(pv), r, v))
+    return out
+
+
+def run_ensembles(G, args, rank, barrier):
+    """Config 4 (256 systems, lognormal counts, ~6.2e6 particles): autotuned
+    persistent batched launch vs the same systems run one at a time."""
+    from glisser_gb300.autotune import tune_ensemble
+    cfg = ("Time-Step 180\nTime-Block-Size %d\nFinal-Time 1e30\nCull-Radius 0.5\nOuter-Limit 300\n"
+           "Input-File unused\nOutput-Folder unused\n")
+    probe_sys = ensemble_systems(G, 1.0 / 16, rank)
+
+    def make(T, syst=probe_sys):
+        ens = G.Ensemble(cfg % T, len(syst))
+        for s, (m, pr, pv, r, v) in enumerate(syst):
+            ens.set_system(s, m, pr, pv, r, v)
+        ens.init()
+        return ens
+
+    tune = tune_ensemble(make, time_blocks=(256, 512, 1024), blocks=2)
+    T, cta, ppt = tune["best"]
+    full = ensemble_systems(G, 1.0, rank)
+    ens = make(T, full)
+    ens.set_shape(cta, ppt)
+    for _ in range(args.warmup):
+        ens.step()
+    barrier()
+    s0 = ens.stats()
+    t0 = time.perf_counter()
+    kms = 0.0
+    for _ in range(args.steps):
+        kms += ens.step()
+    el = time.perf_counter() - t0
+    s1 = ens.stats()
+    ps = s1["particle_steps"] - s0["particle_steps"]
+    n_total = sum(len(x[3]) for x in full)
+    del ens
+    # unbatched comparison: each system through the single-system executor
+    # (same T, same starter), on the first 32 systems
+    ps_plain, el_plain = 0, 0.0
+    for m, pr, pv, r, v in full[:32]:
+        sim = G.Simulation(cfg % T)
+        sim.set_planets(m, pr, pv)
+        sim.set_particles(r, v)
+        sim.init()
+        sim.loop()
+        a = sim.stats()["particle_steps"]
+        t1 = time.perf_counter()
+        for _ in range(2):
+            sim.loop()
+        el_plain += time.perf_counter() - t1
+        ps_plain += sim.stats()["particle_steps"] - a
+        del sim
+    return {
+        "workload": "ensembles: 256 systems (Sun + 4 giants, masses x U(0.9,1.1), a x U(0.95,1.05)), lognormal "
+                    "particle counts (median 2e4, clipped 1e3..2e5), %d particles, config-1 distributions, dt=180 d"
+                    % n_total,
+        "value": ps / el, "unit": UNIT, "blocks": args.steps, "time_block": T,
+        "shape": {"threads_per_cta": cta, "particles_per_thread": ppt},
+        "kernel_ms_per_block": kms / args.steps,
+        "autotune": [{"T": a, "cta": b, "ppt": c, "rate": d} for a, b, c, d in tune["table"]],
+        "graph": True, "launches_per_block": (s1["launches"] - s0["launches"]) / args.steps,
+        "unbatched_value": ps_plain / el_plain if el_plain else None,
+        "unbatched_sample": "first 32 systems one at a time through the single-system executor, 2 blocks each",
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -186,6 +263,7 @@ def main():
     ap.add_argument("--sample-particles", type=int, default=65536)
     ap.add_argument("--sample-steps", type=int, default=512)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ensembles", action="store_true")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -310,6 +388,11 @@ def main():
                "sample": "%d particles x %d steps (%.1f s), oracle restatement of MVSKernel::step_forward "
                          "(src/wh.cu:113-177) on %d host threads" % (n_s, args.sample_steps, el, threads)}
 
+    ensembles = None
+    if not args.no_ensembles:
+        del sim
+        ensembles = run_ensembles(G, args, rank, barrier)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -334,6 +417,7 @@ def main():
             "clocks": clk,
             "e2e": e2e,
             "cpu_baseline": cpu,
+            "ensembles": ensembles,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -117,6 +117,19 @@ def lib():
             "glisser_launches": ([P, C.POINTER(C.c_ulonglong)], C.c_int),
             "glisser_l2_flush": ([P, C.c_size_t], C.c_int),
             "glisser_stream": ([P, C.POINTER(P)], C.c_int),
+            "glisser_ensemble_create": ([C.c_char_p, C.c_size_t, C.POINTER(P)], C.c_int),
+            "glisser_ensemble_set_system": ([P, C.c_size_t, C.c_size_t, D, D, D, C.c_size_t, D, D], C.c_int),
+            "glisser_ensemble_set_shape": ([P, C.c_int, C.c_int, C.c_uint32], C.c_int),
+            "glisser_ensemble_set_graph": ([P, C.c_int], C.c_int),
+            "glisser_ensemble_set_starter": ([P, C.c_int], C.c_int),
+            "glisser_ensemble_init": ([P], C.c_int),
+            "glisser_ensemble_step": ([P, D], C.c_int),
+            "glisser_ensemble_counts": ([P, C.c_size_t, SZ, SZ], C.c_int),
+            "glisser_ensemble_get_particles": ([P, C.c_size_t, D, D, U32, U16, C.c_size_t, SZ], C.c_int),
+            "glisser_ensemble_stats": ([P, C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong),
+                                        C.POINTER(C.c_ulonglong)], C.c_int),
+            "glisser_ensemble_time": ([P, D], C.c_int),
+            "glisser_ensemble_destroy": ([P], C.c_int),
             "glisser_partition_noalloc_max_particles": ([], C.c_size_t),
             "glisser_partition_noalloc": ([C.POINTER(ParticlesDev), C.POINTER(ParticlesDev), C.c_size_t, P, P, P],
                                           C.c_int),
@@ -327,6 +340,78 @@ class Simulation:
 
     def write_plhist(self, path, begin=False):
         self._check(lib().glisser_write_plhist(self.h, path.encode(), int(begin)))
+
+
+class Ensemble:
+    """Many independent systems advanced together (one persistent launch per
+    block, replayed from a CUDA graph)."""
+
+    def __init__(self, config_text, n_systems):
+        h = C.c_void_p()
+        rc = lib().glisser_ensemble_create(config_text.encode(), n_systems, C.byref(h))
+        if rc:
+            _raise(rc, last_error())
+        self.h = h
+        self.n_systems = n_systems
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h and _lib is not None:
+            _lib.glisser_ensemble_destroy(h)
+            self.h = None
+
+    def _check(self, rc):
+        if rc:
+            _raise(rc, last_error())
+
+    def set_system(self, s, m, r, v, pr, pv):
+        m = np.ascontiguousarray(m, np.float64)
+        r = np.ascontiguousarray(r, np.float64); v = np.ascontiguousarray(v, np.float64)
+        pr = np.ascontiguousarray(pr, np.float64); pv = np.ascontiguousarray(pv, np.float64)
+        self._check(lib().glisser_ensemble_set_system(self.h, s, len(m), _p(m, D), _p(r, D), _p(v, D), len(pr),
+                                                      _p(pr, D), _p(pv, D)))
+
+    def set_shape(self, cta=128, ppt=1, grid=0):
+        self._check(lib().glisser_ensemble_set_shape(self.h, cta, ppt, grid))
+
+    def set_graph(self, on=True):
+        self._check(lib().glisser_ensemble_set_graph(self.h, int(bool(on))))
+
+    def set_starter(self, starter):
+        self._check(lib().glisser_ensemble_set_starter(self.h, starter))
+
+    def init(self):
+        self._check(lib().glisser_ensemble_init(self.h))
+
+    def step(self):
+        """One time block for every system; returns the block's device ms."""
+        ms = C.c_double()
+        self._check(lib().glisser_ensemble_step(self.h, C.byref(ms)))
+        return ms.value
+
+    def counts(self, s):
+        n, na = C.c_size_t(), C.c_size_t()
+        self._check(lib().glisser_ensemble_counts(self.h, s, C.byref(n), C.byref(na)))
+        return dict(n=n.value, n_alive=na.value)
+
+    def particles(self, s):
+        n = self.counts(s)["n"]
+        r = np.zeros((n, 3)); v = np.zeros((n, 3)); ids = np.zeros(n, np.uint32); fl = np.zeros(n, np.uint16)
+        got = C.c_size_t()
+        self._check(lib().glisser_ensemble_get_particles(self.h, s, _p(r, D), _p(v, D), _p(ids, U32), _p(fl, U16),
+                                                         n, C.byref(got)))
+        return dict(r=r, v=v, id=ids, flags=fl)
+
+    def stats(self):
+        ps, ev, ln = C.c_ulonglong(), C.c_ulonglong(), C.c_ulonglong()
+        lib().glisser_ensemble_stats(self.h, C.byref(ps), C.byref(ev), C.byref(ln))
+        return dict(particle_steps=ps.value, kepler_evals=ev.value, launches=ln.value)
+
+    @property
+    def t(self):
+        x = C.c_double()
+        lib().glisser_ensemble_time(self.h, C.byref(x))
+        return x.value
 
 
 def integrate_timeblock(particles, n_alive, planet_block, params, handoff, stream=0):

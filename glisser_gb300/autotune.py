@@ -1,0 +1,34 @@
+"""Autotuner for the ensemble runner: threads per CTA, particles per thread and
+time-block length.
+
+Each candidate time-block length gets a probe ensemble (the caller's factory,
+normally every system with a subsample of its particles); on it every launch
+shape runs a warm-up block and then `blocks` timed blocks, timed on the host
+around the whole block (kernel, uploads and the overlapped host planet work),
+so the choice reflects what a run sees.  The best (T, cta, ppt) by
+particle-steps per second wins.
+"""
+import time
+
+SHAPES = ((64, 1), (128, 1), (256, 1), (64, 2), (128, 2), (256, 2))
+
+
+def tune_ensemble(make_probe, time_blocks=(256, 512, 1024), shapes=SHAPES, blocks=2):
+    """make_probe(T) -> an initialised glisser_gb300.Ensemble with Time-Block-Size T.
+    Returns dict(best=(T, cta, ppt), rate=..., table=[(T, cta, ppt, rate), ...])."""
+    table = []
+    for T in time_blocks:
+        ens = make_probe(T)
+        for cta, ppt in shapes:
+            ens.set_shape(cta, ppt)
+            ens.step()                              # warm-up (captures the graph)
+            ps0 = ens.stats()["particle_steps"]
+            t0 = time.perf_counter()
+            for _ in range(blocks):
+                ens.step()
+            el = time.perf_counter() - t0
+            rate = (ens.stats()["particle_steps"] - ps0) / el
+            table.append((T, cta, ppt, rate))
+        del ens
+    best = max(table, key=lambda x: x[3])
+    return dict(best=best[:3], rate=best[3], table=table)

@@ -454,3 +454,152 @@ int glisser_to_elements(double mu, const double* r3, const double* v3, int* esig
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Ensembles
+
+#include "ensemble.h"
+
+struct glisser_ensemble_s {
+    std::unique_ptr<glisser::Ensemble> e;
+};
+
+namespace {
+
+template <typename F>
+int guarded_e(F&& f)
+{
+    try {
+        return f();
+    } catch (const std::exception& ex) {
+        g_last_error = ex.what();
+        return code_for(ex);
+    } catch (...) {
+        g_last_error = "unknown error";
+        return GLISSER_E_RUNTIME;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int glisser_ensemble_create(const char* config_text, size_t n_systems, glisser_ensemble_t** out)
+{
+    if (!config_text || !out) return fail(nullptr, GLISSER_E_INVALID, "glisser_ensemble_create: null argument");
+    *out = nullptr;
+    return guarded_e([&] {
+        glisser::Config cfg = glisser::parse_config(config_text, nullptr);
+        std::unique_ptr<glisser_ensemble_s> h(new glisser_ensemble_s());
+        h->e.reset(new glisser::Ensemble(cfg, n_systems));
+        *out = h.release();
+        return GLISSER_OK;
+    });
+}
+
+int glisser_ensemble_set_system(glisser_ensemble_t* e, size_t s, size_t npl, const double* m, const double* r,
+                                const double* v, size_t n, const double* pr, const double* pv)
+{
+    if (!e || npl < 1 || !m || !r || !v || (n && (!pr || !pv)))
+        return fail(nullptr, GLISSER_E_INVALID, "glisser_ensemble_set_system: bad arguments");
+    return guarded_e([&] {
+        e->e->set_system(s, npl, m, r, v, n, pr, pv);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_ensemble_set_shape(glisser_ensemble_t* e, int cta, int ppt, uint32_t grid)
+{
+    if (!e) return GLISSER_E_INVALID;
+    return guarded_e([&] {
+        e->e->set_shape(cta, ppt, grid);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_ensemble_set_graph(glisser_ensemble_t* e, int use_graph)
+{
+    if (!e) return GLISSER_E_INVALID;
+    e->e->set_graph(use_graph != 0);
+    return GLISSER_OK;
+}
+
+int glisser_ensemble_set_starter(glisser_ensemble_t* e, int starter)
+{
+    if (!e || starter < GLISSER_STARTER_CLASSIC || starter > GLISSER_STARTER_SERIES)
+        return fail(nullptr, GLISSER_E_INVALID, "glisser_ensemble_set_starter: classic or series");
+    e->e->set_starter(starter);
+    return GLISSER_OK;
+}
+
+int glisser_ensemble_init(glisser_ensemble_t* e)
+{
+    if (!e) return GLISSER_E_INVALID;
+    return guarded_e([&] {
+        e->e->init();
+        return GLISSER_OK;
+    });
+}
+
+int glisser_ensemble_step(glisser_ensemble_t* e, double* gpu_ms)
+{
+    if (!e) return GLISSER_E_INVALID;
+    return guarded_e([&] {
+        e->e->step(gpu_ms);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_ensemble_counts(const glisser_ensemble_t* e, size_t s, size_t* n, size_t* n_alive)
+{
+    if (!e || s >= e->e->systems()) return fail(nullptr, GLISSER_E_INVALID, "glisser_ensemble_counts: bad system");
+    if (n) *n = e->e->count(s);
+    if (n_alive) *n_alive = e->e->alive(s);
+    return GLISSER_OK;
+}
+
+int glisser_ensemble_get_particles(glisser_ensemble_t* e, size_t s, double* r, double* v, uint32_t* id,
+                                   uint16_t* flags, size_t cap, size_t* n)
+{
+    if (!e) return GLISSER_E_INVALID;
+    return guarded_e([&] {
+        std::vector<glisser::Vec3> rr, vv;
+        std::vector<uint32_t> ii;
+        std::vector<uint16_t> ff;
+        e->e->particles(s, rr, vv, ii, ff);
+        if (n) *n = rr.size();
+        if (cap < rr.size()) return fail(nullptr, GLISSER_E_INVALID, "glisser_ensemble_get_particles: buffer too small");
+        for (size_t k = 0; k < rr.size(); k++) {
+            if (r) { r[3 * k] = rr[k].x; r[3 * k + 1] = rr[k].y; r[3 * k + 2] = rr[k].z; }
+            if (v) { v[3 * k] = vv[k].x; v[3 * k + 1] = vv[k].y; v[3 * k + 2] = vv[k].z; }
+            if (id) id[k] = ii[k];
+            if (flags) flags[k] = ff[k];
+        }
+        return GLISSER_OK;
+    });
+}
+
+int glisser_ensemble_stats(const glisser_ensemble_t* e, unsigned long long* particle_steps,
+                           unsigned long long* kepler_evals, unsigned long long* launches)
+{
+    if (!e) return GLISSER_E_INVALID;
+    if (particle_steps) *particle_steps = e->e->particle_steps();
+    if (kepler_evals) *kepler_evals = e->e->kepler_evals();
+    if (launches) *launches = e->e->launches();
+    return GLISSER_OK;
+}
+
+int glisser_ensemble_time(const glisser_ensemble_t* e, double* t)
+{
+    if (!e || !t) return GLISSER_E_INVALID;
+    *t = e->e->t;
+    return GLISSER_OK;
+}
+
+int glisser_ensemble_destroy(glisser_ensemble_t* e)
+{
+    delete e;
+    return GLISSER_OK;
+}
+
+}  // extern "C"

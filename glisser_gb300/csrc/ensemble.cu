@@ -1,0 +1,504 @@
+// Ensemble runner: many independent planetary systems, each with its own
+// planets and particles, integrated block by block in one persistent launch.
+//
+// Per block:
+//   host  : every system's planet WH for the block (a thread pool over
+//           systems) into pinned staging; the (system, tile) work items of
+//           the tiles that still hold alive particles;
+//   device: one CUDA graph per staging parity, captured once: upload of the
+//           planet blocks and the items, reset of the queue and counters, the
+//           persistent batched kernel, counters back to the host;
+//   host  : the hand-off list updates the per-tile alive counts.
+// Dead particles stay in place (skipped inside their tile); tiles with no
+// alive particle leave the queue, so no per-system partition is needed.
+// The planet work of block k+1 overlaps the kernel of block k.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <thread>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "config.h"
+#include "ensemble.h"
+#include "executor.h"
+#include "timeblock.cuh"
+
+namespace glisser {
+
+namespace {
+
+void ck(cudaError_t e, const char* what)
+{
+    if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <typename T>
+T* dmalloc(size_t n, const char* what)
+{
+    void* p = nullptr;
+    ck(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)), what);
+    return static_cast<T*>(p);
+}
+
+template <typename T>
+T* hmalloc(size_t n, const char* what)
+{
+    void* p = nullptr;
+    ck(cudaMallocHost(&p, std::max<size_t>(n, 1) * sizeof(T)), what);
+    return static_cast<T*>(p);
+}
+
+}  // namespace
+
+struct Ensemble::Dev {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t k0 = nullptr, k1 = nullptr;
+    glisser_particles pa{};
+    void* pa_base = nullptr;
+    // per parity: planet blocks and items (device + pinned)
+    double* d_log[2] = {};
+    double* d_m[2] = {};
+    double* d_rh[2] = {};
+    uint32_t* d_id[2] = {};
+    BatchItem* d_items[2] = {};
+    uint32_t* d_nitems[2] = {};
+    double* h_log[2] = {};
+    double* h_m[2] = {};
+    double* h_rh[2] = {};
+    uint32_t* h_id[2] = {};
+    BatchItem* h_items[2] = {};
+    uint32_t* h_nitems[2] = {};
+    uint32_t* d_ctr = nullptr;      // [0] hand-off count, [1] status, [2] queue
+    unsigned long long* d_evals = nullptr;
+    uint32_t* h_ctr = nullptr;
+    unsigned long long* h_evals = nullptr;
+    uint32_t *d_ho_index = nullptr, *d_ho_id = nullptr, *d_ho_dti = nullptr;
+    uint16_t* d_ho_flags = nullptr;
+    uint32_t *h_ho_index = nullptr, *h_ho_dti = nullptr;
+    uint16_t* h_ho_flags = nullptr;
+    cudaGraphExec_t graph[2] = {};
+    BatchShape graph_shape[2] = {};
+    uint32_t graph_len[2] = {};
+
+    ~Dev()
+    {
+        for (int b = 0; b < 2; b++) {
+            if (graph[b]) cudaGraphExecDestroy(graph[b]);
+            cudaFree(d_log[b]); cudaFree(d_m[b]); cudaFree(d_rh[b]); cudaFree(d_id[b]);
+            cudaFree(d_items[b]); cudaFree(d_nitems[b]);
+            cudaFreeHost(h_log[b]); cudaFreeHost(h_m[b]); cudaFreeHost(h_rh[b]); cudaFreeHost(h_id[b]);
+            cudaFreeHost(h_items[b]); cudaFreeHost(h_nitems[b]);
+        }
+        cudaFree(pa_base);
+        cudaFree(d_ctr); cudaFree(d_evals); cudaFree(d_ho_index); cudaFree(d_ho_id); cudaFree(d_ho_dti);
+        cudaFree(d_ho_flags);
+        cudaFreeHost(h_ctr); cudaFreeHost(h_evals); cudaFreeHost(h_ho_index); cudaFreeHost(h_ho_dti);
+        cudaFreeHost(h_ho_flags);
+        if (k0) cudaEventDestroy(k0);
+        if (k1) cudaEventDestroy(k1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+Ensemble::Ensemble(const Config& c, size_t n_systems) : cfg(c), sys_(n_systems), dev_(new Dev())
+{
+    if (n_systems == 0) throw std::invalid_argument("an ensemble needs at least one system");
+    shape_ = BatchShape{ 128, 1, 0 };
+}
+
+Ensemble::~Ensemble() = default;
+
+void Ensemble::set_system(size_t s, size_t npl, const double* m, const double* r, const double* v, size_t n,
+                          const double* pr, const double* pv)
+{
+    if (initialized_) throw std::runtime_error("systems can only be set before init");
+    if (s >= sys_.size()) throw std::invalid_argument("system index out of range");
+    System& y = sys_[s];
+    y.pl.resize(npl);
+    y.pl.n_alive = npl;
+    for (size_t i = 0; i < npl; i++) {
+        y.pl.m[i] = m[i] * cfg.big_g;
+        y.pl.r[i] = Vec3{ r[3 * i], r[3 * i + 1], r[3 * i + 2] };
+        y.pl.v[i] = Vec3{ v[3 * i], v[3 * i + 1], v[3 * i + 2] };
+        y.pl.id[i] = (uint32_t)i;
+    }
+    y.r.resize(n);
+    y.v.resize(n);
+    for (size_t k = 0; k < n; k++) {
+        y.r[k] = Vec3{ pr[3 * k], pr[3 * k + 1], pr[3 * k + 2] };
+        y.v[k] = Vec3{ pv[3 * k], pv[3 * k + 1], pv[3 * k + 2] };
+    }
+    y.set = true;
+}
+
+void Ensemble::set_shape(int cta, int ppt, uint32_t grid)
+{
+    if (!(cta == 64 || cta == 128 || cta == 256) || !(ppt == 1 || ppt == 2))
+        throw std::invalid_argument("shape: cta must be 64, 128 or 256 and ppt 1 or 2");
+    if (initialized_ && (uint32_t)(cta * ppt) != tile_) rebuild_tiles(cta * ppt);
+    shape_ = BatchShape{ cta, ppt, grid };
+}
+
+// Planet block of one system for the next cur_len steps (host, one thread).
+void Ensemble::planet_block(size_t s, int par)
+{
+    Dev& d = *dev_;
+    System& y = sys_[s];
+    const uint32_t npl = npl_;
+    y.integ.encounter_radii(y.pl, cfg.cull_radius, cfg.encounter_sphere_factor, y.rh);
+    double* log = d.h_log[par] + s * log_stride_;
+    for (uint32_t k = 0; k < len_; k++) {
+        Vec3 h0 = y.integ.step(y.pl, cfg.dt);
+        double* rec = log + (size_t)k * 3 * npl;
+        rec[0] = h0.x; rec[1] = h0.y; rec[2] = h0.z;
+        for (uint32_t j = 1; j < npl; j++) {
+            rec[3 * j] = y.pl.r[j].x;
+            rec[3 * j + 1] = y.pl.r[j].y;
+            rec[3 * j + 2] = y.pl.r[j].z;
+        }
+    }
+    for (uint32_t j = 0; j < npl; j++) {
+        d.h_m[par][s * npl + j] = y.pl.m[j];
+        d.h_rh[par][s * npl + j] = y.rh[j];
+        d.h_id[par][s * npl + j] = y.pl.id[j];
+    }
+}
+
+void Ensemble::planets_all(int par)
+{
+    const size_t S = sys_.size();
+    unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    size_t nth = std::min<size_t>(hw, S);
+    std::atomic<size_t> next{ 0 };
+    std::vector<std::exception_ptr> errs(nth);
+    auto work = [&](size_t w) {
+        try {
+            for (size_t s = next++; s < S; s = next++) planet_block(s, par);
+        } catch (...) {
+            errs[w] = std::current_exception();
+        }
+    };
+    std::vector<std::thread> th;
+    for (size_t w = 1; w < nth; w++) th.emplace_back(work, w);
+    work(0);
+    for (auto& t : th) t.join();
+    for (auto& e : errs)
+        if (e) std::rethrow_exception(e);
+}
+
+void Ensemble::rebuild_tiles(uint32_t tile)
+{
+    tile_ = tile;
+    tile_alive_.clear();
+    tile_first_.clear();
+    tile_sys_.clear();
+    for (size_t s = 0; s < sys_.size(); s++) {
+        const System& y = sys_[s];
+        for (size_t f = 0; f < y.n; f += tile) {
+            uint32_t cnt = (uint32_t)std::min<size_t>(tile, y.n - f);
+            uint32_t alive = 0;
+            for (uint32_t q = 0; q < cnt; q++) alive += flags_[y.start + f + q] == 0;
+            tile_first_.push_back((uint32_t)(y.start + f));
+            tile_sys_.push_back((uint32_t)s);
+            tile_alive_.push_back(alive);
+            (void)cnt;
+        }
+    }
+}
+
+uint32_t Ensemble::write_items(int par)
+{
+    Dev& d = *dev_;
+    uint32_t k = 0;
+    for (size_t t = 0; t < tile_first_.size(); t++) {
+        if (tile_alive_[t] == 0) continue;
+        const System& y = sys_[tile_sys_[t]];
+        uint32_t end = (uint32_t)(y.start + y.n);
+        d.h_items[par][k++] = BatchItem{ tile_sys_[t], tile_first_[t], std::min(tile_, end - tile_first_[t]), 0 };
+    }
+    *d.h_nitems[par] = k;
+    return k;
+}
+
+void Ensemble::init()
+{
+    if (initialized_) throw std::runtime_error("init called twice");
+    for (auto& y : sys_)
+        if (!y.set) throw std::runtime_error("every system must be set before init");
+    npl_ = (uint32_t)sys_[0].pl.n;
+    for (auto& y : sys_)
+        if (y.pl.n != npl_) throw std::runtime_error("all systems of an ensemble need the same planet count");
+    if (npl_ < 1 || npl_ > (uint32_t)MAX_PLANETS) throw StateError("planet count out of range");
+    len_ = cfg.tbsize;
+    if (len_ == 0) throw std::runtime_error("Time-Block-Size must be positive");
+    Dev& d = *dev_;
+
+    // heliocentric states, planet integrators, start accelerations (the
+    // reference's WHIntegrator ctor, src/wh.cpp:498-577)
+    size_t total = 0;
+    for (auto& y : sys_) {
+        y.start = total;
+        y.n = y.r.size();
+        total += y.n;
+    }
+    n_ = total;
+    std::vector<double> col(9 * std::max<size_t>(total, 1));
+    flags_.assign(total, 0);
+    ids_.resize(total);
+    for (size_t s = 0; s < sys_.size(); s++) {
+        System& y = sys_[s];
+        Vec3 r0 = y.pl.r[0], v0 = y.pl.v[0];
+        for (size_t i = 0; i < y.pl.n; i++) {
+            y.pl.r[i] -= r0;
+            y.pl.v[i] -= v0;
+        }
+        y.integ.init(y.pl);
+        y.integ.encounter_radii(y.pl, cfg.cull_radius, cfg.encounter_sphere_factor, y.rh);
+        Vec3 h0 = y.integ.accelerations(y.pl);
+        for (size_t k = 0; k < y.n; k++) {
+            size_t g = y.start + k;
+            Vec3 r = y.r[k] - r0, v = y.v[k] - v0;
+            Vec3 a = h0;
+            uint16_t fl = 0;
+            for (size_t j = 1; j < y.pl.n_alive; j++) {
+                Vec3 dr = r - y.pl.r[j];
+                double r2 = dr.lensq();
+                double irij3 = 1. / (r2 * std::sqrt(r2));
+                a -= dr * (y.pl.m[j] * irij3);
+                if (r2 < y.rh[j] * y.rh[j]) fl = (uint16_t)((j << 8) | 0x0001);
+            }
+            double r2 = r.lensq();
+            if (r2 < y.rh[0] * y.rh[0]) fl = 0x0001;
+            if (r2 > cfg.outer_radius * cfg.outer_radius) fl = 0x0002;
+            double* c = col.data();
+            c[g] = r.x; c[total + g] = r.y; c[2 * total + g] = r.z;
+            c[3 * total + g] = v.x; c[4 * total + g] = v.y; c[5 * total + g] = v.z;
+            c[6 * total + g] = a.x; c[7 * total + g] = a.y; c[8 * total + g] = a.z;
+            // a particle inside an encounter radius at start is removed at the
+            // first block end, as the executor's KillEncounter does
+            flags_[g] = (fl & 0x01) ? (uint16_t)((fl & 0xFF00) | 0x80) : fl;
+            ids_[g] = (uint32_t)k;
+        }
+        alive_.push_back(0);
+        for (size_t k = 0; k < y.n; k++) alive_.back() += flags_[y.start + k] == 0;
+    }
+
+    ck(cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking), "stream");
+    ck(cudaEventCreate(&d.k0), "event");
+    ck(cudaEventCreate(&d.k1), "event");
+    size_t cap = std::max<size_t>(total, 1);
+    size_t bytes = cap * (9 * sizeof(double) + 2 * sizeof(uint32_t) + sizeof(uint16_t)) + 1024;
+    ck(cudaMalloc(&d.pa_base, bytes), "cudaMalloc particles");
+    char* q = static_cast<char*>(d.pa_base);
+    double** dbl[9] = { &d.pa.rx, &d.pa.ry, &d.pa.rz, &d.pa.vx, &d.pa.vy, &d.pa.vz, &d.pa.ax, &d.pa.ay, &d.pa.az };
+    for (int k = 0; k < 9; k++) {
+        *dbl[k] = reinterpret_cast<double*>(q);
+        q += cap * sizeof(double);
+    }
+    d.pa.deathtime_index = reinterpret_cast<uint32_t*>(q);
+    q += cap * sizeof(uint32_t);
+    d.pa.id = reinterpret_cast<uint32_t*>(q);
+    q += cap * sizeof(uint32_t);
+    d.pa.flags = reinterpret_cast<uint16_t*>(q);
+    for (int k = 0; k < 9; k++)
+        ck(cudaMemcpy(*dbl[k], col.data() + k * total, total * sizeof(double), cudaMemcpyHostToDevice), "upload");
+    ck(cudaMemcpy(d.pa.flags, flags_.data(), total * sizeof(uint16_t), cudaMemcpyHostToDevice), "upload flags");
+    ck(cudaMemcpy(d.pa.id, ids_.data(), total * sizeof(uint32_t), cudaMemcpyHostToDevice), "upload ids");
+    ck(cudaMemset(d.pa.deathtime_index, 0, total * sizeof(uint32_t)), "memset");
+
+    // planet blocks: per system stride rounded to 16 bytes
+    uint32_t recs = (len_ + 1u) & ~1u;
+    log_stride_ = (size_t)recs * 3 * npl_;
+    log_stride_ = (log_stride_ + 1) & ~(size_t)1;
+    size_t S = sys_.size();
+    size_t max_tiles = total / 64 + S + 1;
+    for (int b = 0; b < 2; b++) {
+        d.d_log[b] = dmalloc<double>(S * log_stride_, "cudaMalloc log");
+        d.d_m[b] = dmalloc<double>(S * npl_, "cudaMalloc m");
+        d.d_rh[b] = dmalloc<double>(S * npl_, "cudaMalloc rh");
+        d.d_id[b] = dmalloc<uint32_t>(S * npl_, "cudaMalloc id");
+        d.d_items[b] = dmalloc<BatchItem>(max_tiles, "cudaMalloc items");
+        d.d_nitems[b] = dmalloc<uint32_t>(1, "cudaMalloc items");
+        d.h_log[b] = hmalloc<double>(S * log_stride_, "pinned log");
+        std::memset(d.h_log[b], 0, S * log_stride_ * sizeof(double));
+        d.h_m[b] = hmalloc<double>(S * npl_, "pinned");
+        d.h_rh[b] = hmalloc<double>(S * npl_, "pinned");
+        d.h_id[b] = hmalloc<uint32_t>(S * npl_, "pinned");
+        d.h_items[b] = hmalloc<BatchItem>(max_tiles, "pinned");
+        d.h_nitems[b] = hmalloc<uint32_t>(1, "pinned");
+    }
+    d.d_ctr = dmalloc<uint32_t>(8, "cudaMalloc counters");
+    d.d_evals = dmalloc<unsigned long long>(1, "cudaMalloc evals");
+    d.h_ctr = hmalloc<uint32_t>(8, "pinned");
+    d.h_evals = hmalloc<unsigned long long>(1, "pinned");
+    d.d_ho_index = dmalloc<uint32_t>(cap, "cudaMalloc hand-off");
+    d.d_ho_id = dmalloc<uint32_t>(cap, "cudaMalloc hand-off");
+    d.d_ho_dti = dmalloc<uint32_t>(cap, "cudaMalloc hand-off");
+    d.d_ho_flags = dmalloc<uint16_t>(cap, "cudaMalloc hand-off");
+    d.h_ho_index = hmalloc<uint32_t>(cap, "pinned");
+    d.h_ho_dti = hmalloc<uint32_t>(cap, "pinned");
+    d.h_ho_flags = hmalloc<uint16_t>(cap, "pinned");
+    rebuild_tiles(shape_.cta * shape_.ppt);
+    initialized_ = true;
+    par_ = 0;
+    planets_all(par_);
+}
+
+// Enqueues one block on the stream: uploads, counter reset, kernel, counters back.
+void Ensemble::enqueue(int par)
+{
+    Dev& d = *dev_;
+    const size_t S = sys_.size();
+    ck(cudaMemcpyAsync(d.d_log[par], d.h_log[par], S * log_stride_ * sizeof(double), cudaMemcpyHostToDevice,
+                       d.stream), "upload log");
+    ck(cudaMemcpyAsync(d.d_m[par], d.h_m[par], S * npl_ * sizeof(double), cudaMemcpyHostToDevice, d.stream), "m");
+    ck(cudaMemcpyAsync(d.d_rh[par], d.h_rh[par], S * npl_ * sizeof(double), cudaMemcpyHostToDevice, d.stream), "rh");
+    ck(cudaMemcpyAsync(d.d_id[par], d.h_id[par], S * npl_ * sizeof(uint32_t), cudaMemcpyHostToDevice, d.stream), "id");
+    size_t max_tiles = n_ / 64 + S + 1;
+    ck(cudaMemcpyAsync(d.d_items[par], d.h_items[par], max_tiles * sizeof(BatchItem), cudaMemcpyHostToDevice,
+                       d.stream), "items");
+    ck(cudaMemcpyAsync(d.d_nitems[par], d.h_nitems[par], sizeof(uint32_t), cudaMemcpyHostToDevice, d.stream), "n");
+    ck(cudaMemsetAsync(d.d_ctr, 0, 8 * sizeof(uint32_t), d.stream), "memset");
+    ck(cudaMemsetAsync(d.d_evals, 0, sizeof(unsigned long long), d.stream), "memset");
+    BatchSystems sy{ d.d_log[par], log_stride_, d.d_m[par], d.d_rh[par], d.d_id[par] };
+    glisser_step_params sp{};
+    sp.dt = cfg.dt;
+    sp.outer_radius = cfg.outer_radius;
+    sp.starter = starter_;
+    sp.kill_encounters = 1;
+    sp.mlp = nullptr;
+    glisser_handoff ho{};
+    ho.count = d.d_ctr;
+    ho.status = d.d_ctr + 1;
+    ho.index = d.d_ho_index;
+    ho.id = d.d_ho_id;
+    ho.flags = d.d_ho_flags;
+    ho.deathtime_index = d.d_ho_dti;
+    ho.capacity = (uint32_t)std::max<size_t>(n_, 1);
+    ho.evals = d.d_evals;
+    int rc = launch_batched(&d.pa, sy, d.d_items[par], d.d_nitems[par], d.d_ctr + 2, npl_, len_, &sp, &ho, shape_,
+                            d.stream);
+    if (rc != GLISSER_OK) throw CudaError(std::string("batched launch failed: ") + timeblock_error());
+    ck(cudaMemcpyAsync(d.h_ctr, d.d_ctr, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, d.stream), "counters");
+    ck(cudaMemcpyAsync(d.h_evals, d.d_evals, sizeof(unsigned long long), cudaMemcpyDeviceToHost, d.stream), "evals");
+}
+
+double Ensemble::step(double* gpu_ms)
+{
+    if (!initialized_) throw std::runtime_error("step before init");
+    Dev& d = *dev_;
+    const int par = par_;
+    uint32_t nitems = write_items(par);
+    uint64_t before_alive = 0;
+    for (auto a : alive_) before_alive += a;
+    if (nitems > 0) {
+        if (shape_.grid == 0) shape_.grid = default_grid();
+        ck(cudaEventRecord(d.k0, d.stream), "event");
+        if (use_graph_) {
+            const BatchShape& gs = d.graph_shape[par];
+            bool stale = !d.graph[par] || gs.cta != shape_.cta || gs.ppt != shape_.ppt || gs.grid != shape_.grid ||
+                         d.graph_len[par] != len_;
+            if (stale) {
+                if (d.graph[par]) cudaGraphExecDestroy(d.graph[par]);
+                d.graph[par] = nullptr;
+                cudaGraph_t g;
+                ck(cudaStreamBeginCapture(d.stream, cudaStreamCaptureModeRelaxed), "begin capture");
+                enqueue(par);
+                ck(cudaStreamEndCapture(d.stream, &g), "end capture");
+                ck(cudaGraphInstantiate(&d.graph[par], g, 0), "instantiate");
+                cudaGraphDestroy(g);
+                d.graph_len[par] = len_;
+                d.graph_shape[par] = shape_;
+            }
+            ck(cudaGraphLaunch(d.graph[par], d.stream), "graph launch");
+            launches_ += 1;
+        } else {
+            enqueue(par);
+            launches_ += 1;
+        }
+        ck(cudaEventRecord(d.k1, d.stream), "event");
+    }
+    // the next block's planets while the kernel runs
+    t += cfg.dt * len_;
+    par_ ^= 1;
+    planets_all(par_);
+    float ms = 0;
+    if (nitems > 0) {
+        ck(cudaStreamSynchronize(d.stream), "block");
+        ck(cudaEventElapsedTime(&ms, d.k0, d.k1), "elapsed");
+        if (d.h_ctr[1]) throw CudaError("batched kernel reported a planet-log staging timeout");
+        uint32_t k = std::min<uint32_t>(d.h_ctr[0], (uint32_t)std::max<size_t>(n_, 1));
+        evals_ += *d.h_evals;
+        uint64_t dti_sum = 0;
+        if (k) {
+            ck(cudaMemcpy(d.h_ho_index, d.d_ho_index, k * sizeof(uint32_t), cudaMemcpyDeviceToHost), "hand-off");
+            ck(cudaMemcpy(d.h_ho_dti, d.d_ho_dti, k * sizeof(uint32_t), cudaMemcpyDeviceToHost), "hand-off");
+            ck(cudaMemcpy(d.h_ho_flags, d.d_ho_flags, k * sizeof(uint16_t), cudaMemcpyDeviceToHost), "hand-off");
+            for (uint32_t q = 0; q < k; q++) {
+                uint32_t g = d.h_ho_index[q];
+                bool was_alive = flags_[g] == 0;
+                flags_[g] = d.h_ho_flags[q];
+                dti_sum += d.h_ho_dti[q];
+                if (was_alive && flags_[g] != 0) {
+                    // locate the tile and the system of particle g
+                    size_t t = std::upper_bound(tile_first_.begin(), tile_first_.end(), g) - tile_first_.begin() - 1;
+                    tile_alive_[t]--;
+                    alive_[tile_sys_[t]]--;
+                }
+            }
+        }
+        uint64_t after_alive = 0;
+        for (auto a : alive_) after_alive += a;
+        // survivors advanced the whole block, the newly flagged their index
+        psteps_ += (before_alive - (before_alive - after_alive)) * (uint64_t)len_ + dti_sum;
+        host_dirty_ = true;
+    }
+    if (gpu_ms) *gpu_ms = ms;
+    return ms;
+}
+
+void Ensemble::particles(size_t s, std::vector<Vec3>& r, std::vector<Vec3>& v, std::vector<uint32_t>& id,
+                         std::vector<uint16_t>& flags)
+{
+    if (s >= sys_.size()) throw std::invalid_argument("system index out of range");
+    if (!initialized_) throw std::runtime_error("particles before init");
+    Dev& d = *dev_;
+    const System& y = sys_[s];
+    std::vector<double> c(6 * y.n);
+    double* src[6] = { d.pa.rx, d.pa.ry, d.pa.rz, d.pa.vx, d.pa.vy, d.pa.vz };
+    ck(cudaStreamSynchronize(d.stream), "sync");
+    for (int k = 0; k < 6; k++)
+        ck(cudaMemcpy(c.data() + k * y.n, src[k] + y.start, y.n * sizeof(double), cudaMemcpyDeviceToHost), "download");
+    r.resize(y.n);
+    v.resize(y.n);
+    id.resize(y.n);
+    flags.resize(y.n);
+    ck(cudaMemcpy(id.data(), d.pa.id + y.start, y.n * sizeof(uint32_t), cudaMemcpyDeviceToHost), "download ids");
+    ck(cudaMemcpy(flags.data(), d.pa.flags + y.start, y.n * sizeof(uint16_t), cudaMemcpyDeviceToHost), "download");
+    for (size_t k = 0; k < y.n; k++) {
+        r[k] = Vec3{ c[k], c[y.n + k], c[2 * y.n + k] };
+        v[k] = Vec3{ c[3 * y.n + k], c[4 * y.n + k], c[5 * y.n + k] };
+    }
+}
+
+// One wave of persistent CTAs at the occupancy the kernel reaches.
+uint32_t Ensemble::default_grid() const
+{
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int regs_per_thread = 128;    // the tile routine's register budget
+    int per_sm = std::max(1, 65536 / (regs_per_thread * shape_.cta));
+    return (uint32_t)(sms * per_sm);
+}
+
+size_t Ensemble::alive(size_t s) const { return s < alive_.size() ? alive_[s] : 0; }
+size_t Ensemble::count(size_t s) const { return s < sys_.size() ? sys_[s].r.size() : 0; }
+
+}  // namespace glisser

@@ -1,0 +1,77 @@
+// Ensemble runner: many independent planetary systems in one persistent
+// launch per time block (see ensemble.cu).
+#pragma once
+#include <cstdint>
+#include <memory>
+#include <vector>
+
+#include "config.h"
+#include "planets.h"
+#include "timeblock.cuh"
+
+namespace glisser {
+
+class Ensemble {
+public:
+    Ensemble(const Config& cfg, size_t n_systems);
+    ~Ensemble();
+    Ensemble(const Ensemble&) = delete;
+    Ensemble& operator=(const Ensemble&) = delete;
+
+    Config cfg;
+    double t = 0;
+
+    // planets [npl] including the Sun, particles [n]; vectors are [.][3]
+    void set_system(size_t s, size_t npl, const double* m, const double* r, const double* v, size_t n,
+                    const double* pr, const double* pv);
+    void set_shape(int cta, int ppt, uint32_t grid);
+    BatchShape shape() const { return shape_; }
+    void set_time_block(uint32_t len) { len_ = len; }
+    uint32_t time_block() const { return len_; }
+    void set_graph(bool on) { use_graph_ = on; }
+    void set_starter(int s) { starter_ = s; }
+    void init();
+    double step(double* gpu_ms);    // one block for every system
+
+    size_t systems() const { return sys_.size(); }
+    size_t alive(size_t s) const;
+    size_t count(size_t s) const;
+    void particles(size_t s, std::vector<Vec3>& r, std::vector<Vec3>& v, std::vector<uint32_t>& id,
+                   std::vector<uint16_t>& flags);
+    unsigned long long particle_steps() const { return psteps_; }
+    unsigned long long kepler_evals() const { return evals_; }
+    unsigned long long launches() const { return launches_; }
+
+private:
+    struct System {
+        Planets pl;
+        PlanetIntegrator integ;
+        std::vector<double> rh;
+        std::vector<Vec3> r, v;     // start state (host)
+        size_t start = 0, n = 0;
+        bool set = false;
+    };
+    std::vector<System> sys_;
+    struct Dev;
+    std::unique_ptr<Dev> dev_;
+    BatchShape shape_{};
+    uint32_t npl_ = 0, len_ = 0, tile_ = 0;
+    size_t n_ = 0, log_stride_ = 0;
+    int par_ = 0;
+    int starter_ = GLISSER_STARTER_SERIES;
+    bool initialized_ = false, use_graph_ = true, host_dirty_ = false;
+    std::vector<uint16_t> flags_;
+    std::vector<uint32_t> ids_;
+    std::vector<uint32_t> tile_first_, tile_sys_, tile_alive_;
+    std::vector<uint64_t> alive_;
+    unsigned long long psteps_ = 0, evals_ = 0, launches_ = 0;
+
+    void planet_block(size_t s, int par);
+    void planets_all(int par);
+    void rebuild_tiles(uint32_t tile);
+    uint32_t write_items(int par);
+    void enqueue(int par);
+    uint32_t default_grid() const;
+};
+
+}  // namespace glisser

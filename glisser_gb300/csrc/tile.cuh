@@ -1,0 +1,321 @@
+// Tile routine shared by the single-system and the ensemble time-block
+// kernels (see timeblock.cu for the design).  Header-only: every function is
+// device inline or host inline, compiled into each kernel translation unit.
+#pragma once
+#include "kepler.cuh"
+#include "timeblock.cuh"
+
+namespace glisser {
+namespace tile {
+
+struct Common {
+    glisser_particles pa;
+    uint32_t npl;
+    uint32_t len;
+    uint32_t chunk;
+    double dt;
+    double outer2;
+    int starter;
+    int kill;
+    const MlpDev* mlp;
+    glisser_handoff ho;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Bounded wait: ~2^22 polls (each poll may itself suspend briefly).
+constexpr uint32_t WAIT_POLLS = 1u << 22;
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity)
+{
+    for (uint32_t k = 0; k < WAIT_POLLS; k++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// Issues the copy of log chunk c into `buf`.  Bytes are rounded up to an
+// even number of steps; the caller guarantees capacity for it.
+__device__ __forceinline__ void issue_chunk(const Common& p, const double* log, double* buf, uint64_t* bar,
+                                            uint32_t c, uint32_t rec)
+{
+    uint32_t first = c * p.chunk;
+    uint32_t steps = min(p.chunk, p.len - first);
+    steps = (steps + 1u) & ~1u;
+    uint32_t bytes = steps * rec * 8u;
+    mbar_expect_tx(bar, bytes);
+    bulk_copy_g2s(buf, log + (size_t)first * rec, bytes, bar);
+}
+
+// Acceleration from planet j and its encounter test (src/wh.cu:145-160):
+// the first planet inside its radius wins (flags == 0 guard).
+__device__ __forceinline__ void planet_kick(const double* L, int j, double rx, double ry, double rz, double& ax,
+                                            double& ay, double& az, uint16_t& flags, const double* s_m,
+                                            const double* s_rh2, const uint32_t* s_id)
+{
+    double dx = rx - L[3 * j];
+    double dy = ry - L[3 * j + 1];
+    double dz = rz - L[3 * j + 2];
+    double rad = fma(dx, dx, fma(dy, dy, dz * dz));
+    if (lt_nonneg(rad, s_rh2[j]) && flags == 0) flags = (uint16_t)((s_id[j] << 8) | 0x0001);
+    double inv = rsqrt_fast46(rad);
+    double fac = s_m[j] * (inv * inv * inv);
+    ax = fma(-dx, fac, ax);
+    ay = fma(-dy, fac, ay);
+    az = fma(-dz, fac, az);
+}
+
+// Shared-memory state of one CTA.
+struct CtaShared {
+    double m[MAX_PLANETS];
+    double rh2[MAX_PLANETS];
+    uint32_t id[MAX_PLANETS];
+    uint64_t bar[2];
+    int abort;
+    uint32_t item;
+};
+
+// Integrates particles first + k*CTA + tid (k < PPT, below first + count)
+// of one system over the block, staging that system's log through the two
+// buffers.  `phase` counts completed waits per buffer (identical in every
+// thread; carried across tiles of a persistent CTA).  Returns false after a
+// staging timeout.
+template <int NP, int CTA, int PPT>
+__device__ __forceinline__ bool run_tile(const Common& p, const double* log, uint32_t first, uint32_t count,
+                                         double* stage, CtaShared& sh, uint32_t* phase)
+{
+    const int np = NP > 0 ? NP : (int)p.npl - 1;
+    const uint32_t rec = 3u * (uint32_t)(np + 1);
+    const size_t bufstride = (size_t)p.chunk * rec;
+    const uint32_t tid = threadIdx.x;
+    const uint32_t nchunks = (p.len + p.chunk - 1) / p.chunk;
+    bool inflight0 = false, inflight1 = false;   // thread 0 only
+    if (tid == 0) {
+        if (nchunks > 0) { issue_chunk(p, log, stage, &sh.bar[0], 0, rec); inflight0 = true; }
+        if (nchunks > 1) { issue_chunk(p, log, stage + bufstride, &sh.bar[1], 1, rec); inflight1 = true; }
+    }
+
+    double rx[PPT], ry[PPT], rz[PPT], vx[PPT], vy[PPT], vz[PPT], ax[PPT], ay[PPT], az[PPT], r2[PPT];
+    uint16_t flags[PPT], flags0[PPT];
+    uint32_t dti[PPT];
+    uint32_t evals = 0;
+    const double hdt = p.dt * 0.5;
+    const double mu = sh.m[0];
+    const double dt2mu = p.dt * p.dt * mu;
+    const double rh2_sun = sh.rh2[0];
+#pragma unroll
+    for (int k = 0; k < PPT; k++) {
+        const uint32_t off = (uint32_t)k * CTA + tid;
+        const uint32_t i = first + off;
+        rx[k] = ry[k] = rz[k] = vx[k] = vy[k] = vz[k] = ax[k] = ay[k] = az[k] = 0;
+        flags[k] = 0xFFFF;
+        if (off < count) {
+            rx[k] = p.pa.rx[i]; ry[k] = p.pa.ry[i]; rz[k] = p.pa.rz[i];
+            vx[k] = p.pa.vx[i]; vy[k] = p.pa.vy[i]; vz[k] = p.pa.vz[i];
+            ax[k] = p.pa.ax[i]; ay[k] = p.pa.ay[i]; az[k] = p.pa.az[i];
+            flags[k] = p.pa.flags[i];
+        }
+        flags0[k] = flags[k];
+        dti[k] = 0;
+        // Kick-drift-kick with the two half kicks between consecutive steps
+        // merged into one full kick (v += a dt); a particle takes the closing
+        // half kick when it is flagged or the block ends, so its stored
+        // velocity is always at a step boundary.  |r|^2 from the Sun/outer
+        // test is the next drift's r0^2.
+        if (flags[k] == 0 && p.len > 0) {
+            vx[k] = fma(ax[k], hdt, vx[k]);
+            vy[k] = fma(ay[k], hdt, vy[k]);
+            vz[k] = fma(az[k], hdt, vz[k]);
+        }
+        r2[k] = fma(rx[k], rx[k], fma(ry[k], ry[k], rz[k] * rz[k]));
+    }
+
+    bool ok = true;
+    for (uint32_t c = 0; c < nchunks; c++) {
+        const uint32_t b = c & 1u;
+        if (!sh.abort) {
+            if (!mbar_wait_bounded(&sh.bar[b], phase[b] & 1u)) {
+                sh.abort = 1;
+                atomicOr(p.ho.status, GLISSER_STATUS_LOG_TIMEOUT);
+            }
+        }
+        __syncthreads();
+        if (sh.abort) {
+            ok = false;
+            break;
+        }
+        phase[b]++;
+        if (tid == 0) {
+            if (b == 0) inflight0 = false;
+            else inflight1 = false;
+        }
+        const double* L0 = stage + b * bufstride;
+        const uint32_t cfirst = c * p.chunk;
+        const uint32_t steps = min(p.chunk, p.len - cfirst);
+        for (uint32_t s = 0; s < steps; s++) {
+            const double* L = L0 + (size_t)s * rec;
+#pragma unroll
+            for (int k = 0; k < PPT; k++) {
+                if (flags[k] != 0) continue;
+                DriftResult d = kepler_drift(rx[k], ry[k], rz[k], vx[k], vy[k], vz[k], r2[k], p.dt, mu, dt2mu,
+                                             p.starter, p.mlp);
+                uint16_t fl = d.flags;
+                evals += d.evals;
+                double aax = L[0], aay = L[1], aaz = L[2];
+                if constexpr (NP > 0) {
+#pragma unroll
+                    for (int j = 1; j <= NP; j++)
+                        planet_kick(L, j, rx[k], ry[k], rz[k], aax, aay, aaz, fl, sh.m, sh.rh2, sh.id);
+                } else {
+                    for (int j = 1; j <= np; j++)
+                        planet_kick(L, j, rx[k], ry[k], rz[k], aax, aay, aaz, fl, sh.m, sh.rh2, sh.id);
+                }
+                double rr = fma(rx[k], rx[k], fma(ry[k], ry[k], rz[k] * rz[k]));
+                if (lt_nonneg(rr, rh2_sun)) fl = 0x0001;
+                if (gt_nonneg(rr, p.outer2)) fl = 0x0002;
+                r2[k] = rr;
+                flags[k] = fl;
+                ax[k] = aax; ay[k] = aay; az[k] = aaz;
+                dti[k] = cfirst + s + 1;
+                const double kc = (fl != 0 || dti[k] == p.len) ? hdt : p.dt;
+                vx[k] = fma(aax, kc, vx[k]);
+                vy[k] = fma(aay, kc, vy[k]);
+                vz[k] = fma(aaz, kc, vz[k]);
+            }
+        }
+        __syncthreads();
+        if (tid == 0 && c + 2 < nchunks) {
+            fence_proxy_async();
+            issue_chunk(p, log, stage + b * bufstride, &sh.bar[b], c + 2, rec);
+            if (b == 0) inflight0 = true;
+            else inflight1 = true;
+        }
+    }
+    if (!ok && tid == 0) {
+        // drain the copies still in flight before the shared memory is reused or released
+        if (inflight0) (void)mbar_wait_bounded(&sh.bar[0], phase[0] & 1u);
+        if (inflight1) (void)mbar_wait_bounded(&sh.bar[1], phase[1] & 1u);
+    }
+
+    const unsigned lane = tid & 31u;
+#pragma unroll
+    for (int k = 0; k < PPT; k++) {
+        const uint32_t off = (uint32_t)k * CTA + tid;
+        const uint32_t i = first + off;
+        const bool active = off < count;
+        if (active) {
+            if (p.kill && (flags[k] & 0x01)) flags[k] = (uint16_t)((flags[k] & 0xFF00) | 0x80);
+            p.pa.rx[i] = rx[k]; p.pa.ry[i] = ry[k]; p.pa.rz[i] = rz[k];
+            p.pa.vx[i] = vx[k]; p.pa.vy[i] = vy[k]; p.pa.vz[i] = vz[k];
+            p.pa.ax[i] = ax[k]; p.pa.ay[i] = ay[k]; p.pa.az[i] = az[k];
+            p.pa.flags[i] = flags[k];
+            p.pa.deathtime_index[i] = dti[k];
+        }
+        // hand-off compaction: one atomic per warp
+        const bool changed = active && flags[k] != flags0[k];
+        const unsigned ballot = __ballot_sync(0xffffffffu, changed);
+        if (ballot) {
+            const unsigned leader = __ffs(ballot) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(p.ho.count, (uint32_t)__popc(ballot));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (changed) {
+                uint32_t slot = base + __popc(ballot & ((1u << lane) - 1u));
+                if (slot < p.ho.capacity) {
+                    p.ho.index[slot] = i;
+                    p.ho.id[slot] = p.pa.id[i];
+                    p.ho.flags[slot] = flags[k];
+                    p.ho.deathtime_index[slot] = dti[k];
+                }
+            }
+        }
+    }
+    if (p.ho.evals) {
+        unsigned long long e = evals;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
+        if (lane == 0 && e) atomicAdd(p.ho.evals, e);
+    }
+    return ok;
+}
+
+__device__ __forceinline__ void load_planet_constants(CtaShared& sh, uint32_t npl, const double* m, const double* rh,
+                                                      const uint32_t* pid)
+{
+    for (uint32_t j = threadIdx.x; j < npl; j += blockDim.x) {
+        sh.m[j] = m[j];
+        sh.rh2[j] = rh[j] * rh[j];
+        sh.id[j] = pid[j];
+    }
+}
+
+__device__ __forceinline__ void init_barriers(CtaShared& sh)
+{
+    if (threadIdx.x == 0) {
+        sh.abort = 0;
+        mbar_init(&sh.bar[0], 1);
+        mbar_init(&sh.bar[1], 1);
+        mbar_fence_init();
+    }
+}
+
+
+inline bool fill_common(Common& p, const glisser_particles* pa, const glisser_step_params* sp, const glisser_handoff* ho,
+                 uint32_t npl, uint32_t len)
+{
+    p.pa = *pa;
+    p.npl = npl;
+    p.len = len;
+    p.dt = sp->dt;
+    p.outer2 = sp->outer_radius * sp->outer_radius;
+    p.starter = sp->starter;
+    p.kill = sp->kill_encounters;
+    p.mlp = reinterpret_cast<const MlpDev*>(sp->mlp);
+    if (p.starter == STARTER_LEARNED && !p.mlp) p.starter = STARTER_SERIES;
+    p.ho = *ho;
+    p.chunk = log_chunk_steps(npl);
+    return p.chunk >= 2;
+}
+
+inline bool handoff_ok(const glisser_handoff* ho)
+{
+    if (!ho->count || !ho->status) return false;
+    return !(ho->capacity && (!ho->index || !ho->id || !ho->flags || !ho->deathtime_index));
+}
+
+}  // namespace tile
+}  // namespace glisser

@@ -83,8 +83,27 @@ def workload(cfg_id, n=None, seed=0):
     return c
 
 
-def ensemble_counts(systems=256, median=20000, clip=(1000, 200000), sigma=1.0, seed=0):
-    """Lognormal particle counts per system (config 4)."""
+def ensemble_counts(systems=256, median=20000, clip=(1000, 200000), sigma=0.6, seed=0):
+    """Lognormal particle counts per system (config 4; sigma 0.6 gives ~6e6
+    particles over 256 systems)."""
     rng = np.random.default_rng(seed)
     c = np.exp(rng.normal(np.log(median), sigma, systems))
     return np.clip(np.round(c), clip[0], clip[1]).astype(np.int64)
+
+
+def ensemble_workload(systems=256, seed=0, fraction=1.0, counts=None):
+    """Config 4: per system (planet masses [5], planet elements [4, 6],
+    particle elements [n, 6]); giant masses x U(0.9, 1.1) and semi-major axes
+    x U(0.95, 1.05) per system, particles with the config-1 distributions.
+    Sub-seed per system = seed + system index.  `fraction` keeps that share of
+    every system's particles (at least one)."""
+    if counts is None:
+        counts = ensemble_counts(systems, seed=seed)
+    out = []
+    for s in range(systems):
+        rng = np.random.default_rng(seed + s)
+        m, pel = giant_planets(rng, mass_scale=rng.uniform(0.9, 1.1, 4), a_scale=rng.uniform(0.95, 1.05, 4))
+        n = max(1, int(round(counts[s] * fraction)))
+        el = particle_elements(rng, n, (40, 50), (0, 0.1), 5.0)
+        out.append((m, pel, el))
+    return out

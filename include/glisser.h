@@ -224,6 +224,35 @@ int glisser_stats(const glisser_t *h, unsigned long long *particle_steps, unsign
 int glisser_launches(const glisser_t *h, unsigned long long *launches);
 int glisser_stream(const glisser_t *h, void **stream);
 
+/* ------------------------------------------------------------------------
+ * Ensembles: many independent planetary systems (each its own planets and
+ * particles, one shared configuration: Time-Step, Time-Block-Size,
+ * Outer-Limit, Cull-Radius, Encounter-RH-Factor, Big-G) advanced together,
+ * one persistent kernel launch per time block, replayed from a CUDA graph.
+ * No reference counterpart: the reference runs one system per process.
+ * Errors: glisser_last_error_global.
+ * ---------------------------------------------------------------------- */
+typedef struct glisser_ensemble_s glisser_ensemble_t;
+int glisser_ensemble_create(const char *config_text, size_t n_systems, glisser_ensemble_t **out);
+/* System s: npl planets (Sun first; every system the same npl), n particles;
+ * vectors are [.][3] in any inertial frame. */
+int glisser_ensemble_set_system(glisser_ensemble_t *e, size_t s, size_t npl, const double *m, const double *r,
+                                const double *v, size_t n, const double *pr, const double *pv);
+/* Launch shape: threads per CTA (64, 128, 256), particles per thread (1, 2),
+ * persistent CTAs (0 = one full wave).  May change between blocks. */
+int glisser_ensemble_set_shape(glisser_ensemble_t *e, int cta, int ppt, uint32_t grid);
+int glisser_ensemble_set_graph(glisser_ensemble_t *e, int use_graph);
+int glisser_ensemble_set_starter(glisser_ensemble_t *e, int starter);
+int glisser_ensemble_init(glisser_ensemble_t *e);
+int glisser_ensemble_step(glisser_ensemble_t *e, double *gpu_ms);
+int glisser_ensemble_counts(const glisser_ensemble_t *e, size_t s, size_t *n, size_t *n_alive);
+int glisser_ensemble_get_particles(glisser_ensemble_t *e, size_t s, double *r, double *v, uint32_t *id,
+                                   uint16_t *flags, size_t cap, size_t *n);
+int glisser_ensemble_stats(const glisser_ensemble_t *e, unsigned long long *particle_steps,
+                           unsigned long long *kepler_evals, unsigned long long *launches);
+int glisser_ensemble_time(const glisser_ensemble_t *e, double *t);
+int glisser_ensemble_destroy(glisser_ensemble_t *e);
+
 /* Element conversions (src/convert.cpp:257-497). */
 int glisser_from_elements_M(double mu, double a, double e, double i, double capom, double om, double M,
                             double *r3, double *v3);
