@@ -187,6 +187,51 @@ def ensemble_systems(G, fraction, rank, n_systems=256):
     return out
 
 
+def run_ensembles_learned(G, args, cfg, full, shape, barrier):
+    """Learned starter on the ensemble: trained on plain-method solves logged
+    from the first 16 systems (4 blocks each, one Simulation per system),
+    then the whole ensemble timed with the learned starter."""
+    import tempfile
+    from glisser_gb300 import learned as L
+    subset = full[:16]
+    tr = L.Trainer(sum(len(x[3]) for x in subset) * 4 + 1, seed=5)
+    t0 = time.perf_counter()
+    for m, pr, pv, r, v in subset:
+        sim = G.Simulation(cfg)
+        sim.set_planets(m, pr, pv)
+        sim.set_particles(r, v)
+        sim.init()
+        for _ in range(4):
+            tr.log_simulation(sim)
+            sim.loop()
+        del sim
+    tr.fit_norm()
+    losses = tr.train(args.learned_train_steps, batch=16384, lr=3e-3, lr_min=1e-5, seed=13)
+    t_train = time.perf_counter() - t0
+    path = os.path.join(tempfile.mkdtemp(), "starter.bin")
+    tr.save(path)
+    ens = G.Ensemble(cfg, len(full))
+    for s, (m, pr, pv, r, v) in enumerate(full):
+        ens.set_system(s, m, pr, pv, r, v)
+    ens.set_starter(G.STARTER_LEARNED, path)
+    ens.init()
+    ens.set_shape(*shape)
+    for _ in range(args.warmup):
+        ens.step()
+    barrier()
+    s0 = ens.stats()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ens.step()
+    el = time.perf_counter() - t0
+    s1 = ens.stats()
+    ps = s1["particle_steps"] - s0["particle_steps"]
+    del ens
+    return {"value": ps / el, "unit": UNIT, "samples": tr.samples()[0], "log_and_train_s": t_train,
+            "loss_last": float(losses[-100:].mean()),
+            "evals_per_particle_step": (s1["kepler_evals"] - s0["kepler_evals"]) / max(ps, 1)}
+
+
 def run_ensembles(G, args, rank, barrier):
     """Config 4 (256 systems, lognormal counts, ~6.2e6 particles): autotuned
     persistent batched launch vs the same systems run one at a time."""
@@ -220,6 +265,7 @@ def run_ensembles(G, args, rank, barrier):
     ps = s1["particle_steps"] - s0["particle_steps"]
     n_total = sum(len(x[3]) for x in full)
     del ens
+    learned = run_ensembles_learned(G, args, cfg % T, full, (cta, ppt), barrier)
     # unbatched comparison: each system through the single-system executor
     # (same T, same starter), on the first 32 systems
     ps_plain, el_plain = 0, 0.0
@@ -245,8 +291,97 @@ def run_ensembles(G, args, rank, barrier):
         "kernel_ms_per_block": kms / args.steps,
         "autotune": [{"T": a, "cta": b, "ppt": c, "rate": d} for a, b, c, d in tune["table"]],
         "graph": True, "launches_per_block": (s1["launches"] - s0["launches"]) / args.steps,
+        "evals_per_particle_step": (s1["kepler_evals"] - s0["kepler_evals"]) / max(ps, 1),
+        "learned": learned,
         "unbatched_value": ps_plain / el_plain if el_plain else None,
         "unbatched_sample": "first 32 systems one at a time through the single-system executor, 2 blocks each",
+    }
+
+
+def run_learned(G, args, rank, barrier):
+    """Scattered-disk workload (Sun + Neptune-mass planet; a~logU(30,1000) au,
+    e~U(0,0.95), i~U(0,40deg); Outer-Limit 1e5 au): log the plain method's
+    Kepler solves over `learned_log_blocks` blocks, train the starter on the
+    GPU, then time the same start state with the classic (reference), series
+    and learned starters."""
+    import tempfile
+    import torch
+    from glisser_gb300 import learned as L
+    from glisser_gb300 import synth
+    T = 512
+    dt = 180.0
+    cfg = config_text(T, dt, outer=1e5)
+    m, pr, pv, r, v = synth.cartesian_state(3, args.learned_particles, seed=2000 + rank)
+
+    def make(starter, path=None):
+        sim = G.Simulation(cfg)
+        sim.set_planets(m, pr, pv)
+        sim.set_particles(r, v)
+        sim.set_starter(starter, path)
+        sim.init()
+        return sim
+
+    tr = L.Trainer(args.learned_particles * args.learned_log_blocks + 1, seed=7)
+    sim = make(G.STARTER_SERIES)
+    t0 = time.perf_counter()
+    for _ in range(args.learned_log_blocks):
+        tr.log_simulation(sim)
+        sim.loop()
+    t_log = time.perf_counter() - t0
+    del sim
+    n_samples, plain_evals = tr.samples()
+    tr.fit_norm()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    losses = tr.train(args.learned_train_steps, batch=16384, lr=3e-3, lr_min=1e-5, seed=11)
+    t_train = time.perf_counter() - t0
+    path = os.path.join(tempfile.mkdtemp(), "starter.bin")
+    tr.save(path)
+
+    legs = {}
+    finals = {}
+    for name, st in (("classic", G.STARTER_CLASSIC), ("series", G.STARTER_SERIES), ("learned", G.STARTER_LEARNED)):
+        sim = make(st, path if st == G.STARTER_LEARNED else None)
+        stream = torch.cuda.ExternalStream(sim.stream())
+        sim.loop()                                  # warm-up block
+        barrier()
+        s0 = sim.stats()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        kms = 0.0
+        for _ in range(args.learned_blocks):
+            kms += sim.loop()[2]
+        e1.record(stream)
+        e1.synchronize()
+        el = e0.elapsed_time(e1) * 1e-3
+        s1 = sim.stats()
+        ps = s1["particle_steps"] - s0["particle_steps"]
+        legs[name] = {"value": ps / el, "unit": UNIT, "kernel_ms_per_block": kms / args.learned_blocks,
+                      "kepler_evals_per_particle_step": (s1["kepler_evals"] - s0["kepler_evals"]) / max(ps, 1)}
+        p = sim.particles()
+        o = np.argsort(p["id"])
+        finals[name] = (p["r"][o], p["flags"][o])
+        del sim
+    ref_r, ref_f = finals["series"]
+    for name in ("classic", "learned"):
+        rr, ff = finals[name]
+        live = (ref_f == 0) & (ff == 0)
+        d = np.linalg.norm(rr - ref_r, axis=1) / np.linalg.norm(ref_r, axis=1)
+        legs[name]["max_rel_pos_diff_vs_series"] = float(d[live].max()) if live.any() else None
+        legs[name]["flags_identical_to_series"] = bool(np.array_equal(ff, ref_f))
+    return {
+        "workload": "scattered-disk: Sun + Neptune-mass planet at 30 au, %d particles a~logU(30,1000) au, "
+                    "e~U(0,0.95), i~U(0,40deg), dt=180 d, Time-Block-Size %d, Outer-Limit 1e5 au"
+                    % (args.learned_particles, T),
+        "blocks": args.learned_blocks, "steps_per_leg": (1 + args.learned_blocks) * T,
+        "training": {"samples": n_samples, "plain_evals_per_solve": plain_evals / max(n_samples, 1),
+                     "log_blocks": args.learned_log_blocks, "log_s": t_log, "steps": args.learned_train_steps,
+                     "batch": 16384, "train_s": t_train, "loss_first": float(losses[:10].mean()),
+                     "loss_last": float(losses[-100:].mean()), "network": "3-32-32-1 SiLU, BF16 weights, FP32 accumulate"},
+        "starters": legs,
+        "learned_vs_classic": legs["learned"]["value"] / legs["classic"]["value"],
+        "learned_vs_series": legs["learned"]["value"] / legs["series"]["value"],
     }
 
 
@@ -258,12 +393,17 @@ def main():
     ap.add_argument("--impl", default="glisser", choices=["glisser", "reference"])
     ap.add_argument("--particles", type=int, default=1_000_000)
     ap.add_argument("--tbsize", type=int, default=2048)
-    ap.add_argument("--starter", default="series", choices=["classic", "series", "learned"])
+    ap.add_argument("--starter", default="series", choices=["classic", "series"])
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--sample-particles", type=int, default=65536)
     ap.add_argument("--sample-steps", type=int, default=512)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ensembles", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--learned-particles", type=int, default=1_000_000)
+    ap.add_argument("--learned-log-blocks", type=int, default=10)
+    ap.add_argument("--learned-train-steps", type=int, default=8000)
+    ap.add_argument("--learned-blocks", type=int, default=3)
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -281,7 +421,7 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     import glisser_gb300 as G
     G.build()
-    starter = {"classic": G.STARTER_CLASSIC, "series": G.STARTER_SERIES, "learned": G.STARTER_LEARNED}[args.starter]
+    starter = {"classic": G.STARTER_CLASSIC, "series": G.STARTER_SERIES}[args.starter]
 
     w, m, pr, pv, r, v = make_state(G, args.particles, 2, rank)
     n_planets = len(m) - 1
@@ -289,8 +429,7 @@ def main():
     sim = G.Simulation(config_text(args.tbsize, dt))
     sim.set_planets(m, pr, pv)
     sim.set_particles(r, v)
-    sim.set_starter(starter, os.path.join(ROOT, "glisser_gb300", "weights", "starter.bin")
-                    if starter == G.STARTER_LEARNED else None)
+    sim.set_starter(starter, None)
     sim.init()
     blk0 = sim.planet_block()
     stream = torch.cuda.ExternalStream(sim.stream(), device=torch.device("cuda", local))
@@ -388,10 +527,13 @@ def main():
                "sample": "%d particles x %d steps (%.1f s), oracle restatement of MVSKernel::step_forward "
                          "(src/wh.cu:113-177) on %d host threads" % (n_s, args.sample_steps, el, threads)}
 
+    del sim
     ensembles = None
     if not args.no_ensembles:
-        del sim
         ensembles = run_ensembles(G, args, rank, barrier)
+    learned = None
+    if not args.no_learned:
+        learned = run_learned(G, args, rank, barrier)
 
     if rank == 0:
         line = {
@@ -418,6 +560,7 @@ def main():
             "e2e": e2e,
             "cpu_baseline": cpu,
             "ensembles": ensembles,
+            "learned": learned,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

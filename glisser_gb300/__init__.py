@@ -38,6 +38,7 @@ class EndOfHistory(GlisserError):
 D = C.POINTER(C.c_double)
 U32 = C.POINTER(C.c_uint32)
 U16 = C.POINTER(C.c_uint16)
+F32 = C.POINTER(C.c_float)
 SZ = C.POINTER(C.c_size_t)
 
 
@@ -55,6 +56,14 @@ class PlanetBlockDev(C.Structure):
 class StepParams(C.Structure):
     _fields_ = [("dt", C.c_double), ("outer_radius", C.c_double), ("starter", C.c_int32),
                 ("kill_encounters", C.c_int32), ("mlp", C.c_void_p)]
+
+
+class MlpNorm(C.Structure):
+    """glisser_mlp_norm: feature normalisation, training box and output scale
+    of a learned starter."""
+    _fields_ = [("in_mean", C.c_float * 4), ("in_scale", C.c_float * 4), ("x_lo", C.c_float * 4),
+                ("x_hi", C.c_float * 4), ("out_mean", C.c_float), ("out_scale", C.c_float),
+                ("reserved", C.c_float * 2)]
 
 
 class HandoffDev(C.Structure):
@@ -121,7 +130,7 @@ def lib():
             "glisser_ensemble_set_system": ([P, C.c_size_t, C.c_size_t, D, D, D, C.c_size_t, D, D], C.c_int),
             "glisser_ensemble_set_shape": ([P, C.c_int, C.c_int, C.c_uint32], C.c_int),
             "glisser_ensemble_set_graph": ([P, C.c_int], C.c_int),
-            "glisser_ensemble_set_starter": ([P, C.c_int], C.c_int),
+            "glisser_ensemble_set_starter": ([P, C.c_int, C.c_char_p], C.c_int),
             "glisser_ensemble_init": ([P], C.c_int),
             "glisser_ensemble_step": ([P, D], C.c_int),
             "glisser_ensemble_counts": ([P, C.c_size_t, SZ, SZ], C.c_int),
@@ -130,6 +139,26 @@ def lib():
                                         C.POINTER(C.c_ulonglong)], C.c_int),
             "glisser_ensemble_time": ([P, D], C.c_int),
             "glisser_ensemble_destroy": ([P], C.c_int),
+            "glisser_mlp_create": ([C.c_size_t, C.c_uint64, C.POINTER(P)], C.c_int),
+            "glisser_mlp_destroy": ([P], C.c_int),
+            "glisser_mlp_log_simulation": ([P, P, SZ], C.c_int),
+            "glisser_mlp_log_states": ([P, C.POINTER(ParticlesDev), C.c_size_t, C.c_double, C.c_double, P, SZ],
+                                       C.c_int),
+            "glisser_mlp_add_samples": ([P, F32, F32, C.c_size_t], C.c_int),
+            "glisser_mlp_get_samples": ([P, F32, F32, C.c_size_t, C.c_size_t], C.c_int),
+            "glisser_mlp_samples": ([P, SZ, C.POINTER(C.c_ulonglong)], C.c_int),
+            "glisser_mlp_fit_norm": ([P], C.c_int),
+            "glisser_mlp_get_norm": ([P, C.POINTER(MlpNorm)], C.c_int),
+            "glisser_mlp_set_norm": ([P, C.POINTER(MlpNorm)], C.c_int),
+            "glisser_mlp_get_params": ([P, F32], C.c_int),
+            "glisser_mlp_set_params": ([P, F32], C.c_int),
+            "glisser_mlp_train": ([P, C.c_int, C.c_int, C.c_float, C.c_float, C.c_uint64, F32], C.c_int),
+            "glisser_mlp_gradients": ([P, F32, F32, C.c_size_t, F32, F32], C.c_int),
+            "glisser_mlp_predict": ([P, F32, C.c_size_t, F32], C.c_int),
+            "glisser_mlp_save": ([P, C.c_char_p], C.c_int),
+            "glisser_mlp_device_weights": ([P, C.POINTER(P)], C.c_int),
+            "glisser_kepler_drift_states": ([C.POINTER(ParticlesDev), C.c_size_t, C.c_double, C.c_double, C.c_int,
+                                             P, P, P, P], C.c_int),
             "glisser_partition_noalloc_max_particles": ([], C.c_size_t),
             "glisser_partition_noalloc": ([C.POINTER(ParticlesDev), C.POINTER(ParticlesDev), C.c_size_t, P, P, P],
                                           C.c_int),
@@ -377,8 +406,8 @@ class Ensemble:
     def set_graph(self, on=True):
         self._check(lib().glisser_ensemble_set_graph(self.h, int(bool(on))))
 
-    def set_starter(self, starter):
-        self._check(lib().glisser_ensemble_set_starter(self.h, starter))
+    def set_starter(self, starter, mlp_path=None):
+        self._check(lib().glisser_ensemble_set_starter(self.h, starter, mlp_path.encode() if mlp_path else None))
 
     def init(self):
         self._check(lib().glisser_ensemble_init(self.h))

@@ -1,0 +1,82 @@
+// Ensemble (persistent work-queue) kernel template, included by the
+// translation units that instantiate it (plain starters in batched.cu, the
+// learned starter in batched_learned.cu; disjoint instantiations, internal
+// linkage).
+#pragma once
+#include "tile.cuh"
+
+namespace glisser {
+namespace {
+
+using namespace tile;
+
+// Persistent kernel over (system, tile) work items.
+template <int NP, int CTA, int PPT, bool LEARNED>
+__global__ void __launch_bounds__(CTA)
+    batched_kernel(const Common p, BatchSystems sys, const BatchItem* items, const uint32_t* n_items, uint32_t* queue)
+{
+    extern __shared__ __align__(128) double stage[];
+    __shared__ CtaShared sh;
+    init_barriers(sh);
+    uint32_t phase[2] = { 0, 0 };
+    const uint32_t total = *n_items;
+    for (;;) {
+        if (threadIdx.x == 0) sh.item = atomicAdd(queue, 1u);
+        __syncthreads();
+        const uint32_t it = sh.item;
+        if (it >= total || sh.abort) break;
+        const BatchItem w = items[it];
+        load_planet_constants(sh, p.npl, sys.m + (size_t)w.system * p.npl, sys.rh + (size_t)w.system * p.npl,
+                              sys.id + (size_t)w.system * p.npl);
+        __syncthreads();
+        bool ok = run_tile<NP, CTA, PPT, LEARNED>(p, sys.log + (size_t)w.system * sys.log_stride, w.first, w.count, stage, sh,
+                                         phase);
+        __syncthreads();   // sh.item / planet constants are rewritten by the next item
+        if (!ok) break;
+    }
+}
+
+template <int NP, int CTA, int PPT, bool LEARNED>
+cudaError_t launch_batched_t(const Common& p, const BatchSystems& sys, const BatchItem* items,
+                             const uint32_t* n_items, uint32_t* queue, uint32_t grid, size_t smem,
+                             cudaStream_t stream)
+{
+    auto kern = batched_kernel<NP, CTA, PPT, LEARNED>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    if (grid == 0) {
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, CTA, smem);
+        grid = (uint32_t)(sms * (per > 0 ? per : 1));
+    }
+    kern<<<grid, CTA, smem, stream>>>(p, sys, items, n_items, queue);
+    return cudaGetLastError();
+}
+
+template <int NP, bool LEARNED>
+cudaError_t launch_batched_np(const Common& p, const BatchSystems& sys, const BatchItem* items,
+                              const uint32_t* n_items, uint32_t* queue, const BatchShape& shape, size_t smem,
+                              cudaStream_t stream)
+{
+    const int key = shape.cta * 10 + shape.ppt;
+    switch (key) {
+    case 641: return launch_batched_t<NP, 64, 1, LEARNED>(p, sys, items, n_items, queue, shape.grid, smem, stream);
+    case 642: return launch_batched_t<NP, 64, 2, LEARNED>(p, sys, items, n_items, queue, shape.grid, smem, stream);
+    case 1281: return launch_batched_t<NP, 128, 1, LEARNED>(p, sys, items, n_items, queue, shape.grid, smem, stream);
+    case 1282: return launch_batched_t<NP, 128, 2, LEARNED>(p, sys, items, n_items, queue, shape.grid, smem, stream);
+    case 2561: return launch_batched_t<NP, 256, 1, LEARNED>(p, sys, items, n_items, queue, shape.grid, smem, stream);
+    case 2562: return launch_batched_t<NP, 256, 2, LEARNED>(p, sys, items, n_items, queue, shape.grid, smem, stream);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace
+
+// Learned-starter launch (batched_learned.cu).
+cudaError_t launch_batched_learned(const tile::Common& p, const BatchSystems& sys, const BatchItem* items,
+                                   const uint32_t* n_items, uint32_t* queue, uint32_t npl, const BatchShape& shape,
+                                   size_t smem, cudaStream_t stream);
+
+}  // namespace glisser

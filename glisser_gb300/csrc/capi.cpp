@@ -12,6 +12,7 @@
 #include "../../include/glisser.h"
 #include "config.h"
 #include "executor.h"
+#include "mlp_train.h"
 #include "orbits.h"
 #include "state_io.h"
 #include "timeblock.cuh"
@@ -20,7 +21,6 @@ namespace glisser {
 size_t partition_scratch_bytes(size_t n);
 int launch_partition(const glisser_particles* in, const glisser_particles* out, size_t n, void* scratch,
                      uint32_t* n0, uint32_t* n1, cudaStream_t stream);
-size_t mlp_blob_bytes();
 size_t partition_noalloc_max_particles();
 int launch_partition_noalloc(const glisser_particles* in, const glisser_particles* out, size_t n, uint32_t* n0,
                              uint32_t* n1, cudaStream_t stream);
@@ -34,6 +34,13 @@ struct glisser_s {
 namespace {
 
 thread_local std::string g_last_error;
+
+std::vector<uint8_t> read_file(const char* path)
+{
+    std::ifstream in(path, std::ios::binary);
+    if (!in) throw glisser::IoError(std::string("cannot read ") + path);
+    return std::vector<uint8_t>(std::istreambuf_iterator<char>(in), std::istreambuf_iterator<char>());
+}
 
 int code_for(const std::exception& e)
 {
@@ -208,11 +215,7 @@ int glisser_set_starter(glisser_t* h, int starter, const char* mlp_path)
 {
     return guarded(h, [&] {
         std::vector<uint8_t> blob;
-        if (mlp_path) {
-            std::ifstream in(mlp_path, std::ios::binary);
-            if (!in) throw glisser::IoError(std::string("cannot read ") + mlp_path);
-            blob.assign(std::istreambuf_iterator<char>(in), std::istreambuf_iterator<char>());
-        }
+        if (mlp_path) blob = read_file(mlp_path);
         exec_of(h).set_starter(starter, mlp_path ? &blob : nullptr);
         return GLISSER_OK;
     });
@@ -524,14 +527,16 @@ int glisser_ensemble_set_graph(glisser_ensemble_t* e, int use_graph)
     return GLISSER_OK;
 }
 
-int glisser_ensemble_set_starter(glisser_ensemble_t* e, int starter)
+int glisser_ensemble_set_starter(glisser_ensemble_t* e, int starter, const char* mlp_path)
 {
-    if (!e || starter < GLISSER_STARTER_CLASSIC || starter > GLISSER_STARTER_SERIES)
-        return fail(nullptr, GLISSER_E_INVALID, "glisser_ensemble_set_starter: classic or series");
-    e->e->set_starter(starter);
-    return GLISSER_OK;
+    if (!e) return GLISSER_E_INVALID;
+    return guarded_e([&] {
+        std::vector<uint8_t> blob;
+        if (mlp_path) blob = read_file(mlp_path);
+        e->e->set_starter(starter, mlp_path ? &blob : nullptr);
+        return GLISSER_OK;
+    });
 }
-
 int glisser_ensemble_init(glisser_ensemble_t* e)
 {
     if (!e) return GLISSER_E_INVALID;
@@ -599,6 +604,196 @@ int glisser_ensemble_time(const glisser_ensemble_t* e, double* t)
 int glisser_ensemble_destroy(glisser_ensemble_t* e)
 {
     delete e;
+    return GLISSER_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Learned starter
+
+struct glisser_mlp {
+    std::unique_ptr<glisser::MlpTrainer> t;
+};
+
+extern "C" {
+
+int glisser_mlp_create(size_t capacity, uint64_t seed, glisser_mlp_t** out)
+{
+    if (!out) return fail(nullptr, GLISSER_E_INVALID, "glisser_mlp_create: null argument");
+    *out = nullptr;
+    return guarded_e([&] {
+        std::unique_ptr<glisser_mlp> m(new glisser_mlp());
+        m->t.reset(new glisser::MlpTrainer(capacity, seed));
+        *out = m.release();
+        return GLISSER_OK;
+    });
+}
+
+int glisser_mlp_destroy(glisser_mlp_t* m)
+{
+    delete m;
+    return GLISSER_OK;
+}
+
+int glisser_mlp_log_simulation(glisser_mlp_t* m, glisser_t* h, size_t* n_logged)
+{
+    if (!m || !h) return fail(nullptr, GLISSER_E_INVALID, "glisser_mlp_log_simulation: null argument");
+    return guarded_e([&] {
+        glisser_particles pa;
+        size_t n = 0;
+        double dt = 0, mu = 0;
+        exec_of(h).device_view(&pa, &n, &dt, &mu);
+        size_t k = n ? m->t->log_states(pa, n, dt, mu, (cudaStream_t)exec_of(h).stream()) : 0;
+        if (n_logged) *n_logged = k;
+        return GLISSER_OK;
+    });
+}
+
+int glisser_mlp_log_states(glisser_mlp_t* m, const glisser_particles* pa, size_t n, double dt, double mu,
+                           void* stream, size_t* n_logged)
+{
+    if (!m || !pa || !(dt > 0) || !(mu > 0)) return fail(nullptr, GLISSER_E_INVALID, "glisser_mlp_log_states: bad arguments");
+    return guarded_e([&] {
+        size_t k = m->t->log_states(*pa, n, dt, mu, (cudaStream_t)stream);
+        if (n_logged) *n_logged = k;
+        return GLISSER_OK;
+    });
+}
+
+int glisser_mlp_add_samples(glisser_mlp_t* m, const float* feat, const float* target, size_t n)
+{
+    if (!m || (n && (!feat || !target))) return fail(nullptr, GLISSER_E_INVALID, "glisser_mlp_add_samples: bad arguments");
+    return guarded_e([&] {
+        m->t->add_samples(feat, target, n);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_mlp_get_samples(const glisser_mlp_t* m, float* feat, float* target, size_t first, size_t n)
+{
+    if (!m) return GLISSER_E_INVALID;
+    return guarded_e([&] {
+        m->t->get_samples(feat, target, first, n);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_mlp_samples(glisser_mlp_t* m, size_t* n, unsigned long long* plain_evals)
+{
+    if (!m) return GLISSER_E_INVALID;
+    return guarded_e([&] {
+        if (n) *n = m->t->samples();
+        if (plain_evals) *plain_evals = m->t->plain_evals();
+        return GLISSER_OK;
+    });
+}
+
+int glisser_mlp_fit_norm(glisser_mlp_t* m)
+{
+    if (!m) return GLISSER_E_INVALID;
+    return guarded_e([&] {
+        m->t->fit_norm();
+        return GLISSER_OK;
+    });
+}
+
+int glisser_mlp_get_norm(const glisser_mlp_t* m, glisser_mlp_norm* out)
+{
+    if (!m || !out) return GLISSER_E_INVALID;
+    *out = m->t->norm;
+    return GLISSER_OK;
+}
+
+int glisser_mlp_set_norm(glisser_mlp_t* m, const glisser_mlp_norm* in)
+{
+    if (!m || !in) return GLISSER_E_INVALID;
+    return guarded_e([&] {
+        for (int k = 0; k < 3; k++)
+            if (!(in->in_scale[k] > 0) || !(in->x_lo[k] <= in->x_hi[k]))
+                throw std::invalid_argument("glisser_mlp_set_norm: scale must be positive and lo <= hi");
+        if (!(in->out_scale > 0)) throw std::invalid_argument("glisser_mlp_set_norm: out_scale must be positive");
+        float p[GLISSER_MLP_NPARAM];
+        m->t->get_params(p);
+        m->t->norm = *in;
+        m->t->norm_set = true;
+        m->t->set_params(p);   // marks the device copy stale
+        return GLISSER_OK;
+    });
+}
+
+int glisser_mlp_get_params(const glisser_mlp_t* m, float* params)
+{
+    if (!m || !params) return GLISSER_E_INVALID;
+    m->t->get_params(params);
+    return GLISSER_OK;
+}
+
+int glisser_mlp_set_params(glisser_mlp_t* m, const float* params)
+{
+    if (!m || !params) return GLISSER_E_INVALID;
+    return guarded_e([&] {
+        m->t->set_params(params);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_mlp_train(glisser_mlp_t* m, int steps, int batch, float lr, float lr_min, uint64_t seed, float* losses)
+{
+    if (!m || steps < 0 || !(lr > 0) || !(lr_min >= 0)) return fail(nullptr, GLISSER_E_INVALID, "glisser_mlp_train: bad arguments");
+    return guarded_e([&] {
+        m->t->train(steps, batch, lr, lr_min, seed, losses);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_mlp_gradients(glisser_mlp_t* m, const float* feat, const float* target, size_t n, float* grad,
+                          float* loss)
+{
+    if (!m || !feat || !target || !grad || n == 0)
+        return fail(nullptr, GLISSER_E_INVALID, "glisser_mlp_gradients: bad arguments");
+    return guarded_e([&] {
+        m->t->gradients(feat, target, n, grad, loss);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_mlp_predict(glisser_mlp_t* m, const float* feat, size_t n, float* y)
+{
+    if (!m || (n && (!feat || !y))) return fail(nullptr, GLISSER_E_INVALID, "glisser_mlp_predict: bad arguments");
+    return guarded_e([&] {
+        m->t->predict(feat, n, y);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_mlp_save(const glisser_mlp_t* m, const char* path)
+{
+    if (!m || !path) return GLISSER_E_INVALID;
+    return guarded_e([&] {
+        std::vector<uint8_t> b = m->t->file_bytes();
+        std::ofstream o(path, std::ios::binary);
+        if (!o) throw glisser::IoError(std::string("cannot write ") + path);
+        o.write(reinterpret_cast<const char*>(b.data()), (std::streamsize)b.size());
+        if (!o) throw glisser::IoError(std::string("cannot write ") + path);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_mlp_device_weights(glisser_mlp_t* m, const void** dev)
+{
+    if (!m || !dev) return GLISSER_E_INVALID;
+    return guarded_e([&] {
+        *dev = m->t->device_weights();
+        return GLISSER_OK;
+    });
+}
+
+int glisser_kepler_drift_states(const glisser_particles* pa, size_t n, double dt, double mu, int starter,
+                                const void* mlp, uint32_t* evals, uint16_t* flags, void* stream)
+{
+    int rc = glisser::drift_states(pa, n, dt, mu, starter, mlp, evals, flags, (cudaStream_t)stream);
+    if (rc != GLISSER_OK) return fail(nullptr, rc, "glisser_kepler_drift_states: bad arguments or launch failure");
     return GLISSER_OK;
 }
 

@@ -27,6 +27,7 @@
 #include "config.h"
 #include "ensemble.h"
 #include "executor.h"
+#include "mlp_train.h"
 #include "timeblock.cuh"
 
 namespace glisser {
@@ -85,9 +86,13 @@ struct Ensemble::Dev {
     cudaGraphExec_t graph[2] = {};
     BatchShape graph_shape[2] = {};
     uint32_t graph_len[2] = {};
+    int graph_starter[2] = { -1, -1 };
+    void* d_mlp = nullptr;            // learned-starter weights
+    int mlp_version = 0, graph_mlp[2] = { 0, 0 };
 
     ~Dev()
     {
+        mlp_free(d_mlp);
         for (int b = 0; b < 2; b++) {
             if (graph[b]) cudaGraphExecDestroy(graph[b]);
             cudaFree(d_log[b]); cudaFree(d_m[b]); cudaFree(d_rh[b]); cudaFree(d_id[b]);
@@ -113,6 +118,19 @@ Ensemble::Ensemble(const Config& c, size_t n_systems) : cfg(c), sys_(n_systems),
 }
 
 Ensemble::~Ensemble() = default;
+
+void Ensemble::set_starter(int s, const std::vector<uint8_t>* mlp_file)
+{
+    if (s < GLISSER_STARTER_CLASSIC || s > GLISSER_STARTER_LEARNED) throw std::invalid_argument("unknown starter");
+    if (s == GLISSER_STARTER_LEARNED) {
+        if (!mlp_file) throw std::invalid_argument("the learned starter needs a weights file");
+        void* w = mlp_upload(*mlp_file);
+        mlp_free(dev_->d_mlp);
+        dev_->d_mlp = w;
+        dev_->mlp_version++;
+    }
+    starter_ = s;
+}
 
 void Ensemble::set_system(size_t s, size_t npl, const double* m, const double* r, const double* v, size_t n,
                           const double* pr, const double* pv)
@@ -372,7 +390,7 @@ void Ensemble::enqueue(int par)
     sp.outer_radius = cfg.outer_radius;
     sp.starter = starter_;
     sp.kill_encounters = 1;
-    sp.mlp = nullptr;
+    sp.mlp = starter_ == GLISSER_STARTER_LEARNED ? d.d_mlp : nullptr;
     glisser_handoff ho{};
     ho.count = d.d_ctr;
     ho.status = d.d_ctr + 1;
@@ -403,7 +421,8 @@ double Ensemble::step(double* gpu_ms)
         if (use_graph_) {
             const BatchShape& gs = d.graph_shape[par];
             bool stale = !d.graph[par] || gs.cta != shape_.cta || gs.ppt != shape_.ppt || gs.grid != shape_.grid ||
-                         d.graph_len[par] != len_;
+                         d.graph_len[par] != len_ || d.graph_starter[par] != starter_ ||
+                         d.graph_mlp[par] != d.mlp_version;
             if (stale) {
                 if (d.graph[par]) cudaGraphExecDestroy(d.graph[par]);
                 d.graph[par] = nullptr;
@@ -415,6 +434,8 @@ double Ensemble::step(double* gpu_ms)
                 cudaGraphDestroy(g);
                 d.graph_len[par] = len_;
                 d.graph_shape[par] = shape_;
+                d.graph_starter[par] = starter_;
+                d.graph_mlp[par] = d.mlp_version;
             }
             ck(cudaGraphLaunch(d.graph[par], d.stream), "graph launch");
             launches_ += 1;

@@ -29,7 +29,8 @@ public:
     void set_time_block(uint32_t len) { len_ = len; }
     uint32_t time_block() const { return len_; }
     void set_graph(bool on) { use_graph_ = on; }
-    void set_starter(int s) { starter_ = s; }
+    // GLISSER_STARTER_*; the learned starter takes a weights file image
+    void set_starter(int s, const std::vector<uint8_t>* mlp_file);
     void init();
     double step(double* gpu_ms);    // one block for every system
 

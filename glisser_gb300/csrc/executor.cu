@@ -141,6 +141,20 @@ Executor::~Executor() = default;
 
 void* Executor::stream() const { return d_->main; }
 
+void Executor::device_view(glisser_particles* pa, size_t* n, double* dt, double* mu) const
+{
+    if (!initialized_) throw std::invalid_argument("device_view: call init first");
+    if (!d_->device) {
+        *pa = glisser_particles{};
+        *n = 0;
+    } else {
+        *pa = d_->buf[d_->cur].p;
+        *n = n_dev_;
+    }
+    *dt = cur_dt_;
+    *mu = pl_.m[0];
+}
+
 void Executor::load()
 {
     load_state(cfg, pl_, pa_);

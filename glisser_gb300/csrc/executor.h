@@ -65,6 +65,9 @@ public:
     unsigned long long particle_steps() const { return psteps_total_; }
     unsigned long long launches() const { return launches_total_; }
     void* stream() const;
+    // Device state the next block integrates: particles [0, n) (unflagged),
+    // the step and the central mass.
+    void device_view(glisser_particles* pa, size_t* n, double* dt, double* mu) const;
 
     std::ostream* log = nullptr;             // progress / warnings (stdout tee)
     std::ostream* encounter_out = nullptr;   // encounter.out

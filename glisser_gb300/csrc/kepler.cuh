@@ -43,7 +43,7 @@ constexpr int KEP_LAGUERRE_MAX = 200;   // bounded fallback passes
 enum Starter : int {
     STARTER_CLASSIC = 0,   // the reference's kepu_guess (src/wh.cpp:188-220)
     STARTER_SERIES = 1,    // seventh-order time-series reversion, else FP32 Kepler pre-solve
-    STARTER_LEARNED = 2,   // MLP over drift invariants, series fallback
+    STARTER_LEARNED = 2,   // MLP over drift invariants, classic fallback
 };
 
 struct GFun {
@@ -247,8 +247,68 @@ struct DriftResult {
     uint16_t evals;     // Stumpff evaluations spent
 };
 
+// Quartic Newton passes from s (at most KEP_NEWTON_MAX).  On acceptance
+// (|f| < tol at the current s) returns true with the G-functions at s, f''
+// and 1/f' there and the pending Newton correction ds = -f/f'.
+__device__ __forceinline__ bool kepler_newton(double& s, double dt, double r0, double u, double mu, double alpha,
+                                              double k, double tol, GFun& g, double& fpp, double& inv_fp, double& ds,
+                                              uint16_t& evals)
+{
+    for (int it = 0; it < KEP_NEWTON_MAX; it++) {
+        g = gfuns(s, alpha);
+        evals++;
+        double f = fma(r0, g.g1, fma(u, g.g2, fma(mu, g.g3, -dt)));
+        double fp = fma(r0, g.g0, fma(u, g.g1, mu * g.g2));
+        fpp = fma(k, g.g1, u * g.g0);
+        inv_fp = rcp_fast(fp);
+        double h = f * inv_fp;
+        if (lt_nonneg(fabs(f), tol)) {
+            // accepted: a Newton correction is exact to O(h^2) ~ 1e-26
+            ds = -h;
+            return true;
+        }
+        double fppp = fma(k, g.g0, -(u * alpha) * g.g1);
+        double q = fpp * inv_fp;                      // 2A
+        double p = fppp * inv_fp;                     // 6B
+        // quartic step: ds = -h (1 + A h - (B - 2A^2) h^2)
+        double corr = fma(h, fma(-h, fma(p, 1.0 / 6.0, -0.5 * q * q), 0.5 * q), 1.0);
+        s = fma(-h, corr, s);
+    }
+    return false;
+}
+
+// Laguerre's method (n = 5) from s (SWIFT drift_kepu_lag, with the exact
+// f'' = (mu - alpha r0) G1 + u G0), at most KEP_LAGUERRE_MAX passes; same
+// outputs as kepler_newton.
+__device__ __forceinline__ bool kepler_laguerre(double& s, double dt, double r0, double u, double mu, double alpha,
+                                             double k, double tol, GFun& g, double& fpp, double& inv_fp, double& ds,
+                                             uint16_t& evals)
+{
+    const double ln = 5.0;
+    for (int it = 0; it < KEP_LAGUERRE_MAX; it++) {
+        g = gfuns(s, alpha);
+        evals++;
+        double f = fma(r0, g.g1, fma(u, g.g2, fma(mu, g.g3, -dt)));
+        double fp = fma(r0, g.g0, fma(u, g.g1, mu * g.g2));
+        fpp = fma(k, g.g1, u * g.g0);
+        inv_fp = 1.0 / fp;
+        if (fabs(f) < tol) {
+            ds = -f * inv_fp;
+            return true;
+        }
+        double disc = sqrt(fabs((ln - 1.0) * (ln - 1.0) * fp * fp - (ln - 1.0) * ln * f * fpp));
+        s = s - ln * f / (fp + (fp > 0 ? disc : -disc));
+    }
+    return false;
+}
+
 // Drifts (r, v) by dt about a central mass mu.  dt2mu = dt^2 mu (a per-
 // block constant: the step-size test compares tau^2 = dt^2 mu / r0^3).
+// LEARNED selects the MLP starter (weights `mlp`), with the classic starter
+// outside the network's training box and as the restart when the Newton
+// passes from the learned guess do not converge; otherwise `starter` picks
+// the classic or the series starter.
+template <bool LEARNED>
 __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, double& rz, double& vx, double& vy, double& vz,
                                                    double r2, double dt, double mu, double dt2mu, int starter,
                                                    const MlpDev* mlp)
@@ -264,68 +324,33 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
     res.evals = 0;
 
     const double k = fma(-alpha, r0, mu);
+    const double tau2 = dt2mu * (rinv * rinv) * rinv;     // (dt / dynamical time)^2
     double s;
-    if (starter == STARTER_CLASSIC) {
+    if constexpr (LEARNED) {
+        s = starter_learned(mlp, dt, rinv, tau2, u, mu_r, alpha);
+        if (!(s > 0)) s = starter_classic(dt, r0, rinv, mu, alpha, u);
+    } else if (starter == STARTER_CLASSIC) {
         s = starter_classic(dt, r0, rinv, mu, alpha, u);
     } else {
-        s = -1.0;
-        if (starter == STARTER_LEARNED && mlp) s = starter_learned(mlp, dt, r0, rinv, mu, alpha, u);
-        if (!(s > 0)) {
-            double tau2 = dt2mu * (rinv * rinv) * rinv;     // (dt / dynamical time)^2
-            if (lt_nonneg(tau2, 0.0025)) s = starter_series6(dt, rinv, alpha, u, k);
-            else if (alpha > 0) s = starter_fp32_kepler(dt, r0, mu, alpha, u);
-            else s = starter_classic(dt, r0, rinv, mu, alpha, u);
-        }
+        if (lt_nonneg(tau2, 0.0025)) s = starter_series6(dt, rinv, alpha, u, k);
+        else if (alpha > 0) s = starter_fp32_kepler(dt, r0, mu, alpha, u);
+        else s = starter_classic(dt, r0, rinv, mu, alpha, u);
     }
 
     const double tol = KEP_TOL * dt;
     GFun g;
-    double fp = 0, fpp = 0, ds = 0, inv_fp = 0;
-    bool ok = false;
-    for (int it = 0; it < KEP_NEWTON_MAX; it++) {
-        g = gfuns(s, alpha);
-        res.evals++;
-        double f = fma(r0, g.g1, fma(u, g.g2, fma(mu, g.g3, -dt)));
-        fp = fma(r0, g.g0, fma(u, g.g1, mu * g.g2));
-        fpp = fma(k, g.g1, u * g.g0);
-        inv_fp = rcp_fast(fp);
-        double h = f * inv_fp;
-        if (lt_nonneg(fabs(f), tol)) {
-            // accepted: a Newton correction is exact to O(h^2) ~ 1e-26
-            ds = -h;
-            ok = true;
-            break;
-        }
-        double fppp = fma(k, g.g0, -(u * alpha) * g.g1);
-        double q = fpp * inv_fp;                      // 2A
-        double p = fppp * inv_fp;                     // 6B
-        // quartic step: ds = -h (1 + A h - (B - 2A^2) h^2)
-        double corr = fma(h, fma(-h, fma(p, 1.0 / 6.0, -0.5 * q * q), 0.5 * q), 1.0);
-        s = fma(-h, corr, s);
-    }
-    if (!ok) {
-        // Laguerre's method (n = 5) from the last iterate (SWIFT
-        // drift_kepu_lag, with the exact f'' = (mu - alpha r0) G1 + u G0)
-        const double ln = 5.0;
-        for (int it = 0; it < KEP_LAGUERRE_MAX; it++) {
-            g = gfuns(s, alpha);
-            res.evals++;
-            double f = fma(r0, g.g1, fma(u, g.g2, fma(mu, g.g3, -dt)));
-            fp = fma(r0, g.g0, fma(u, g.g1, mu * g.g2));
-            fpp = fma(k, g.g1, u * g.g0);
-            inv_fp = 1.0 / fp;
-            if (fabs(f) < tol) {
-                ds = -f * inv_fp;
-                ok = true;
-                break;
-            }
-            double disc = sqrt(fabs((ln - 1.0) * (ln - 1.0) * fp * fp - (ln - 1.0) * ln * f * fpp));
-            s = s - ln * f / (fp + (fp > 0 ? disc : -disc));
-        }
+    double fpp = 0, ds = 0, inv_fp = 0;
+    bool ok = kepler_newton(s, dt, r0, u, mu, alpha, k, tol, g, fpp, inv_fp, ds, res.evals);
+    if constexpr (LEARNED) {
         if (!ok) {
-            res.flags |= 0x04;
-            ds = 0;
+            s = starter_classic(dt, r0, rinv, mu, alpha, u);
+            ok = kepler_newton(s, dt, r0, u, mu, alpha, k, tol, g, fpp, inv_fp, ds, res.evals);
         }
+    }
+    if (!ok) ok = kepler_laguerre(s, dt, r0, u, mu, alpha, k, tol, g, fpp, inv_fp, ds, res.evals);
+    if (!ok) {
+        res.flags |= 0x04;
+        ds = 0;
     }
     // fold the last correction into the G-functions (dG3 = G2 ds, dG2 =
     // G1 ds, dG1 = G0 ds; |ds| < 1e-13 s, so the second-order terms are

@@ -1,80 +1,125 @@
 // Learned Kepler starter: a 3 -> 32 -> 32 -> 1 MLP with BF16 weights and
 // FP32 accumulation, evaluated per drift inside the time-block kernel.
 //
-// Inputs are dimensionless drift invariants,
-//   x0 = log(tau), tau = dt sqrt(mu / r0^3)      (step over the dynamical time)
-//   x1 = u / sqrt(mu r0)                         (radial velocity)
-//   x2 = alpha r0 / mu                           (binding energy; 2 = circular-ish)
-// and the network predicts y = log(s_hat / tau), s_hat = s sqrt(mu / r0), the
-// universal anomaly over its Keplerian small-step value.  The FP64 Newton
-// iteration after it runs to the same tolerance as with any other starter.
+// Inputs are the dimensionless drift invariants
+//   f0 = log(tau),  tau = dt sqrt(mu / r0^3)      (step over the dynamical time)
+//   f1 = u / sqrt(mu r0),  u = r0 . v0            (radial velocity)
+//   f2 = alpha r0 / mu                            (binding energy; 1 = circular)
+// -- the scaled forms of dt/r0, r0.v0/sqrt(mu r0) and alpha r0, which fix the
+// dimensionless Kepler equation completely -- and the network predicts
+//   z = log(s r0 / dt) / tau,
+// the log of the universal anomaly over its small-step value dt/r0, scaled
+// by tau so that the target stays O(1) (z -> -f1/2 as tau -> 0) and the
+// guess's relative error shrinks with the step.  Hidden units use SiLU.  The FP64 Newton iteration after the guess runs to the same
+// tolerance as with any other starter, so the network only changes how many
+// passes it takes.
+//
+// One forward routine (mlp_forward) serves both the fused inference in the
+// drift and the training kernels, so the network is trained on exactly the
+// arithmetic it is used with: weights hold BF16 values (rounded from the FP32
+// master copy), every product is accumulated in FP32 in a fixed order.
 #pragma once
 #include <cuda_bf16.h>
 #include <cstdint>
+
+#include "../../include/glisser.h"
 
 namespace glisser {
 
 constexpr int MLP_IN = 3;
 constexpr int MLP_H = 32;
 
-// Device-side parameter block (one contiguous allocation).
-struct MlpDev {
-    __nv_bfloat16 w1[MLP_H * MLP_IN];   // [out][in]
-    __nv_bfloat16 w2[MLP_H * MLP_H];
-    __nv_bfloat16 w3[MLP_H];
+// Flattened parameter vector (training and the weights file).
+constexpr int MLP_OFF_W1 = 0;                            // [MLP_H][MLP_IN]
+constexpr int MLP_OFF_B1 = MLP_OFF_W1 + MLP_H * MLP_IN;  // [MLP_H]
+constexpr int MLP_OFF_W2 = MLP_OFF_B1 + MLP_H;           // [MLP_H][MLP_H], [out][in]
+constexpr int MLP_OFF_B2 = MLP_OFF_W2 + MLP_H * MLP_H;
+constexpr int MLP_OFF_W3 = MLP_OFF_B2 + MLP_H;
+constexpr int MLP_OFF_B3 = MLP_OFF_W3 + MLP_H;
+constexpr int MLP_NPARAM = MLP_OFF_B3 + 1;               // 1217
+
+// Normalisation and training box of one network (glisser_mlp_norm):
+// x = (f - in_mean) * in_scale per feature, z = out_mean + out_scale * output.
+using MlpNorm = glisser_mlp_norm;
+
+// Device-resident weights for inference: the BF16 weight values widened to
+// FP32 so that each is one broadcast load, laid out for 16-byte loads.
+struct __align__(16) MlpDev {
+    float w1[MLP_H][4];              // [out][in], input 3 is zero
     float b1[MLP_H];
+    float w2[MLP_H][MLP_H];          // [out][in]
     float b2[MLP_H];
+    float w3[MLP_H];
     float b3;
-    float in_mean[MLP_IN], in_scale[MLP_IN];   // x_norm = (x - mean) * scale
-    float out_mean, out_scale;                 // y = out_mean + y_norm * out_scale
-    float x_lo[MLP_IN], x_hi[MLP_IN];          // training domain (raw features)
     uint32_t valid;
+    float pad[2];
+    MlpNorm norm;
 };
 
-__device__ __forceinline__ float silu_approx(float x) { return x / (1.0f + __expf(-x)); }
+__device__ __forceinline__ float bf16_round(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
 
-// Forward pass in FP32 accumulation over BF16 weights.  Returns the
-// normalised-output prediction y (log ratio), or NaN outside the domain.
-__device__ __forceinline__ float mlp_forward(const MlpDev* __restrict__ w, float f0, float f1, float f2)
+// SiLU and its derivative; the same routine in training and inference.
+__device__ __forceinline__ float mlp_sigmoid(float a) { return __fdividef(1.0f, 1.0f + __expf(-a)); }
+
+// Network output (normalised units) for normalised inputs x0..x2.  Weight
+// rows are read with 16-byte loads; every thread of a warp reads the same
+// address, so each load is one broadcast transaction.
+__device__ __forceinline__ float mlp_forward(const MlpDev* __restrict__ w, float x0, float x1, float x2)
 {
-    float x[MLP_IN] = { f0, f1, f2 };
-#pragma unroll
-    for (int k = 0; k < MLP_IN; k++) {
-        if (!(x[k] >= w->x_lo[k] && x[k] <= w->x_hi[k])) return __int_as_float(0x7fc00000);
-        x[k] = (x[k] - w->in_mean[k]) * w->in_scale[k];
-    }
     float h1[MLP_H];
 #pragma unroll
     for (int j = 0; j < MLP_H; j++) {
-        float a = w->b1[j];
-#pragma unroll
-        for (int k = 0; k < MLP_IN; k++) a = fmaf(__bfloat162float(w->w1[j * MLP_IN + k]), x[k], a);
-        h1[j] = silu_approx(a);
+        const float4 r = __ldg(reinterpret_cast<const float4*>(w->w1[j]));
+        float a = __ldg(&w->b1[j]);
+        a = fmaf(r.x, x0, a);
+        a = fmaf(r.y, x1, a);
+        a = fmaf(r.z, x2, a);
+        h1[j] = a * mlp_sigmoid(a);
     }
-    float y = w->b3;
-#pragma unroll 4
+    float y = __ldg(&w->b3);
+#pragma unroll 2
     for (int j = 0; j < MLP_H; j++) {
-        float a = w->b2[j];
+        float a = __ldg(&w->b2[j]);
+        const float4* row = reinterpret_cast<const float4*>(w->w2[j]);
 #pragma unroll
-        for (int k = 0; k < MLP_H; k++) a = fmaf(__bfloat162float(w->w2[j * MLP_H + k]), h1[k], a);
-        y = fmaf(__bfloat162float(w->w3[j]), silu_approx(a), y);
+        for (int q = 0; q < MLP_H / 4; q++) {
+            const float4 r = __ldg(row + q);
+            a = fmaf(r.x, h1[4 * q], a);
+            a = fmaf(r.y, h1[4 * q + 1], a);
+            a = fmaf(r.z, h1[4 * q + 2], a);
+            a = fmaf(r.w, h1[4 * q + 3], a);
+        }
+        y = fmaf(__ldg(&w->w3[j]), a * mlp_sigmoid(a), y);
     }
-    return w->out_mean + y * w->out_scale;
+    return y;
 }
 
-__device__ __forceinline__ double starter_learned(const MlpDev* mlp, double dt, double r0, double rinv, double mu,
-                                                  double alpha, double u)
+// Raw features of one drift, computed in FP32 from the FP64 invariants
+// (tau2 = dt^2 mu / r0^3, mu_r = mu / r0).
+__device__ __forceinline__ void mlp_features(double tau2, double u, double rinv, double mu_r, double alpha, float& f0,
+                                             float& f1, float& f2)
 {
-    if (!mlp->valid) return -1.0;
-    float sq_mu_r = (float)sqrt(mu * rinv);
-    float tau = (float)(dt * rinv) * sq_mu_r;                 // dt sqrt(mu/r0^3)
-    float f0 = __logf(tau);
-    float f1 = (float)u * (float)rinv / sq_mu_r;              // u / sqrt(mu r0)
-    float f2 = (float)(alpha * r0 / mu);
-    float y = mlp_forward(mlp, f0, f1, f2);
-    if (!(y == y)) return -1.0;
-    float s_hat = tau * __expf(y);
-    return (double)(s_hat / sq_mu_r);                         // s = s_hat / sqrt(mu/r0)
+    const float mr = (float)mu_r;
+    f0 = 0.5f * __logf((float)tau2);
+    f1 = (float)(u * rinv) * rsqrtf(mr);
+    f2 = __fdividef((float)alpha, mr);
+}
+
+// Learned guess for s, or -1 when the drift is outside the training box.
+__device__ __forceinline__ double starter_learned(const MlpDev* __restrict__ w, double dt, double rinv, double tau2,
+                                                  double u, double mu_r, double alpha)
+{
+    float f0, f1, f2;
+    mlp_features(tau2, u, rinv, mu_r, alpha, f0, f1, f2);
+    const MlpNorm& n = w->norm;
+    if (!(f0 >= n.x_lo[0] && f0 <= n.x_hi[0] && f1 >= n.x_lo[1] && f1 <= n.x_hi[1] && f2 >= n.x_lo[2] &&
+          f2 <= n.x_hi[2]))
+        return -1.0;
+    const float x0 = (f0 - n.in_mean[0]) * n.in_scale[0];
+    const float x1 = (f1 - n.in_mean[1]) * n.in_scale[1];
+    const float x2 = (f2 - n.in_mean[2]) * n.in_scale[2];
+    const float z = fmaf(n.out_scale, mlp_forward(w, x0, x1, x2), n.out_mean);
+    return (dt * rinv) * (double)__expf(z * sqrtf((float)tau2));
 }
 
 }  // namespace glisser

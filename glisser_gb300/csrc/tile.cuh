@@ -114,7 +114,7 @@ struct CtaShared {
 // buffers.  `phase` counts completed waits per buffer (identical in every
 // thread; carried across tiles of a persistent CTA).  Returns false after a
 // staging timeout.
-template <int NP, int CTA, int PPT>
+template <int NP, int CTA, int PPT, bool LEARNED>
 __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uint32_t first, uint32_t count,
                                          double* stage, CtaShared& sh, uint32_t* phase)
 {
@@ -191,8 +191,8 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
 #pragma unroll
             for (int k = 0; k < PPT; k++) {
                 if (flags[k] != 0) continue;
-                DriftResult d = kepler_drift(rx[k], ry[k], rz[k], vx[k], vy[k], vz[k], r2[k], p.dt, mu, dt2mu,
-                                             p.starter, p.mlp);
+                DriftResult d = kepler_drift<LEARNED>(rx[k], ry[k], rz[k], vx[k], vy[k], vz[k], r2[k], p.dt, mu, dt2mu,
+                                                       p.starter, p.mlp);
                 uint16_t fl = d.flags;
                 evals += d.evals;
                 double aax = L[0], aay = L[1], aaz = L[2];

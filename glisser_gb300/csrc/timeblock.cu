@@ -25,45 +25,13 @@
 //    chosen by the autotuner.
 #include <cstdio>
 
-#include "tile.cuh"
+#include "timeblock_kernel.cuh"
 
 namespace glisser {
 
 using namespace tile;
 
 namespace {
-
-// CTAs per SM the register allocation is sized for (FP64-pipe bound: more
-// resident warps only help cover FP64 latency)
-#ifndef GLISSER_TB_MIN_BLOCKS
-#define GLISSER_TB_MIN_BLOCKS 4
-#endif
-
-template <int NP>
-__global__ void __launch_bounds__(BLOCK_THREADS, GLISSER_TB_MIN_BLOCKS)
-    timeblock_kernel(const Common p, const double* log, const double* m, const double* rh, const uint32_t* pid,
-                     uint32_t n)
-{
-    extern __shared__ __align__(128) double stage[];
-    __shared__ CtaShared sh;
-    load_planet_constants(sh, p.npl, m, rh, pid);
-    init_barriers(sh);
-    __syncthreads();
-    uint32_t phase[2] = { 0, 0 };
-    const uint32_t first = blockIdx.x * BLOCK_THREADS;
-    run_tile<NP, BLOCK_THREADS, 1>(p, log, first, min((uint32_t)BLOCK_THREADS, n - first), stage, sh, phase);
-}
-
-template <int NP>
-cudaError_t launch_np(const Common& p, const glisser_planet_block* pl, uint32_t n, size_t smem, cudaStream_t stream)
-{
-    auto kern = timeblock_kernel<NP>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    uint32_t grid = (n + BLOCK_THREADS - 1) / BLOCK_THREADS;
-    kern<<<grid, BLOCK_THREADS, smem, stream>>>(p, pl->log, pl->m, pl->rh, pl->id, n);
-    return cudaGetLastError();
-}
 
 thread_local char g_err[256];
 
@@ -102,17 +70,21 @@ int launch_timeblock(const glisser_particles* pa, size_t n_alive, const glisser_
     size_t smem = timeblock_smem_bytes(pl->npl, (int)p.chunk);
     uint32_t n = (uint32_t)n_alive;
     cudaError_t e;
-    switch (pl->npl - 1) {
-    case 0: e = launch_np<0>(p, pl, n, smem, stream); break;
-    case 1: e = launch_np<1>(p, pl, n, smem, stream); break;
-    case 2: e = launch_np<2>(p, pl, n, smem, stream); break;
-    case 3: e = launch_np<3>(p, pl, n, smem, stream); break;
-    case 4: e = launch_np<4>(p, pl, n, smem, stream); break;
-    case 5: e = launch_np<5>(p, pl, n, smem, stream); break;
-    case 6: e = launch_np<6>(p, pl, n, smem, stream); break;
-    case 7: e = launch_np<7>(p, pl, n, smem, stream); break;
-    case 8: e = launch_np<8>(p, pl, n, smem, stream); break;
-    default: e = launch_np<0>(p, pl, n, smem, stream); break;
+    if (sp->starter == GLISSER_STARTER_LEARNED && p.mlp) {
+        e = launch_timeblock_learned(p, pl, n, smem, stream);
+    } else {
+        switch (pl->npl - 1) {
+        case 0: e = launch_np<0, false>(p, pl, n, smem, stream); break;
+        case 1: e = launch_np<1, false>(p, pl, n, smem, stream); break;
+        case 2: e = launch_np<2, false>(p, pl, n, smem, stream); break;
+        case 3: e = launch_np<3, false>(p, pl, n, smem, stream); break;
+        case 4: e = launch_np<4, false>(p, pl, n, smem, stream); break;
+        case 5: e = launch_np<5, false>(p, pl, n, smem, stream); break;
+        case 6: e = launch_np<6, false>(p, pl, n, smem, stream); break;
+        case 7: e = launch_np<7, false>(p, pl, n, smem, stream); break;
+        case 8: e = launch_np<8, false>(p, pl, n, smem, stream); break;
+        default: e = launch_np<0, false>(p, pl, n, smem, stream); break;
+        }
     }
     if (e != cudaSuccess) {
         snprintf(g_err, sizeof g_err, "time-block launch: %s", cudaGetErrorString(e));

@@ -1,0 +1,50 @@
+// Single-system time-block kernel template, included by the translation
+// units that instantiate it (plain starters in timeblock.cu, the learned
+// starter in timeblock_learned.cu; disjoint instantiations, internal linkage).
+#pragma once
+#include "tile.cuh"
+
+namespace glisser {
+namespace {
+
+using namespace tile;
+
+// CTAs per SM the register allocation is sized for (FP64-pipe bound: more
+// resident warps only help cover FP64 latency)
+#ifndef GLISSER_TB_MIN_BLOCKS
+#define GLISSER_TB_MIN_BLOCKS 4
+#endif
+
+template <int NP, bool LEARNED>
+__global__ void __launch_bounds__(BLOCK_THREADS, GLISSER_TB_MIN_BLOCKS)
+    timeblock_kernel(const Common p, const double* log, const double* m, const double* rh, const uint32_t* pid,
+                     uint32_t n)
+{
+    extern __shared__ __align__(128) double stage[];
+    __shared__ CtaShared sh;
+    load_planet_constants(sh, p.npl, m, rh, pid);
+    init_barriers(sh);
+    __syncthreads();
+    uint32_t phase[2] = { 0, 0 };
+    const uint32_t first = blockIdx.x * BLOCK_THREADS;
+    run_tile<NP, BLOCK_THREADS, 1, LEARNED>(p, log, first, min((uint32_t)BLOCK_THREADS, n - first), stage, sh, phase);
+}
+
+template <int NP, bool LEARNED>
+cudaError_t launch_np(const Common& p, const glisser_planet_block* pl, uint32_t n, size_t smem, cudaStream_t stream)
+{
+    auto kern = timeblock_kernel<NP, LEARNED>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    uint32_t grid = (n + BLOCK_THREADS - 1) / BLOCK_THREADS;
+    kern<<<grid, BLOCK_THREADS, smem, stream>>>(p, pl->log, pl->m, pl->rh, pl->id, n);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+// Learned-starter launch (timeblock_learned.cu).
+cudaError_t launch_timeblock_learned(const tile::Common& p, const glisser_planet_block* pl, uint32_t n, size_t smem,
+                                     cudaStream_t stream);
+
+}  // namespace glisser

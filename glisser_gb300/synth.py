@@ -107,3 +107,20 @@ def ensemble_workload(systems=256, seed=0, fraction=1.0, counts=None):
         el = particle_elements(rng, n, (40, 50), (0, 0.1), 5.0)
         out.append((m, pel, el))
     return out
+
+
+def cartesian_state(cfg_id, n, seed, planet_seed=0):
+    """Planets (m [npl], r [npl, 3], v [npl, 3]; Sun at the origin) from the
+    configuration drawn with `planet_seed`, and n particles (r, v [n, 3])
+    drawn with `seed`, heliocentric."""
+    from . import elements_to_cartesian
+    w = workload(cfg_id, n=0, seed=planet_seed)
+    el = workload(cfg_id, n=n, seed=seed)["el"]
+    m = w["pl_m"]
+    pr, pv = [np.zeros(3)], [np.zeros(3)]
+    for k in range(len(m) - 1):
+        a, b = elements_to_cartesian(m[0] + m[k + 1], w["pl_el"][k:k + 1])
+        pr.append(a[0])
+        pv.append(b[0])
+    r, v = elements_to_cartesian(m[0], el)
+    return m, np.array(pr), np.array(pv), r, v

@@ -48,8 +48,19 @@ extern "C" {
 
 /* Kepler starters for the universal-variable drift. */
 #define GLISSER_STARTER_CLASSIC 0  /* the reference's kepu_guess, src/wh.cpp:188-220 */
-#define GLISSER_STARTER_SERIES 1   /* third-order time series / FP32 Kepler pre-solve */
-#define GLISSER_STARTER_LEARNED 2  /* MLP initial guess, series fallback */
+#define GLISSER_STARTER_SERIES 1   /* seventh-order time series / FP32 Kepler pre-solve */
+#define GLISSER_STARTER_LEARNED 2  /* MLP initial guess, classic fallback */
+
+/* Feature normalisation and training box of a learned starter (features
+ * f0 = log(tau), tau = dt sqrt(mu/r0^3), f1 = r0.v0 / sqrt(mu r0),
+ * f2 = alpha r0 / mu; output z = log(s r0 / dt) / tau).  Element 3 of each
+ * array is unused. */
+typedef struct glisser_mlp_norm {
+    float in_mean[4], in_scale[4];   /* x = (f - in_mean) * in_scale */
+    float x_lo[4], x_hi[4];          /* drifts outside this box use the classic starter */
+    float out_mean, out_scale;       /* z = out_mean + out_scale * network output */
+    float reserved[2];
+} glisser_mlp_norm;
 
 /* ------------------------------------------------------------------------
  * Kernel layer.  All pointers in these structs are DEVICE pointers.
@@ -242,7 +253,7 @@ int glisser_ensemble_set_system(glisser_ensemble_t *e, size_t s, size_t npl, con
  * persistent CTAs (0 = one full wave).  May change between blocks. */
 int glisser_ensemble_set_shape(glisser_ensemble_t *e, int cta, int ppt, uint32_t grid);
 int glisser_ensemble_set_graph(glisser_ensemble_t *e, int use_graph);
-int glisser_ensemble_set_starter(glisser_ensemble_t *e, int starter);
+int glisser_ensemble_set_starter(glisser_ensemble_t *e, int starter, const char *mlp_path);
 int glisser_ensemble_init(glisser_ensemble_t *e);
 int glisser_ensemble_step(glisser_ensemble_t *e, double *gpu_ms);
 int glisser_ensemble_counts(const glisser_ensemble_t *e, size_t s, size_t *n, size_t *n_alive);
@@ -269,6 +280,73 @@ int glisser_fp64_peak_probe(double *tflops, double *ms);
  * cudaStream_t) so the next kernel starts with a cold L2; benchmark hygiene,
  * no reference counterpart. */
 int glisser_l2_flush(void *stream, size_t bytes);
+
+/* ------------------------------------------------------------------------
+ * Learned Kepler starter.  No counterpart in the reference (its drift,
+ * src/wh.cu:43-110, always starts Newton from the same analytic guess).  A
+ * 3 -> 32 -> 32 -> 1 MLP with BF16 weights and FP32 accumulation predicts
+ * z = log(s r0 / dt) / tau for the universal anomaly s from three dimensionless
+ * invariants of the drift (glisser_mlp_norm).  It is trained on solves logged
+ * by the plain method, on the GPU, by the library's own forward and backward
+ * kernels; in the drift it only replaces the starting guess of the FP64 Newton
+ * iteration, which runs to the same tolerance as with any other starter.
+ * ---------------------------------------------------------------------- */
+
+#define GLISSER_MLP_NPARAM 1217   /* flattened: W1[32][3] b1[32] W2[32][32] b2[32] w3[32] b3 */
+
+typedef struct glisser_mlp glisser_mlp_t;
+
+/* A trainer with room for `capacity` samples and He-uniform initial weights
+ * drawn from `seed`. */
+int glisser_mlp_create(size_t capacity, uint64_t seed, glisser_mlp_t **out);
+int glisser_mlp_destroy(glisser_mlp_t *m);
+
+/* Logs one sample per unflagged particle of an initialised simulation: the
+ * features of its next drift and the universal anomaly the plain method
+ * (classic starter, FP64 Newton to the drift tolerance) converges to. */
+int glisser_mlp_log_simulation(glisser_mlp_t *m, glisser_t *h, size_t *n_logged);
+/* The same for device states [0, n) (kernel layer; r and v are read). */
+int glisser_mlp_log_states(glisser_mlp_t *m, const glisser_particles *pa, size_t n, double dt, double mu,
+                           void *stream, size_t *n_logged);
+/* Host samples: feat[n][3], target[n] (z; NaN marks a sample to skip). */
+int glisser_mlp_add_samples(glisser_mlp_t *m, const float *feat, const float *target, size_t n);
+int glisser_mlp_get_samples(const glisser_mlp_t *m, float *feat, float *target, size_t first, size_t n);
+/* Samples held, and the Stumpff evaluations the logged plain solves spent. */
+int glisser_mlp_samples(glisser_mlp_t *m, size_t *n, unsigned long long *plain_evals);
+
+/* Normalisation from the held samples (mean / standard deviation of each
+ * feature and of z; the feature box is their min / max). */
+int glisser_mlp_fit_norm(glisser_mlp_t *m);
+int glisser_mlp_get_norm(const glisser_mlp_t *m, glisser_mlp_norm *out);
+int glisser_mlp_set_norm(glisser_mlp_t *m, const glisser_mlp_norm *in);
+int glisser_mlp_get_params(const glisser_mlp_t *m, float *params);   /* [GLISSER_MLP_NPARAM] FP32 master */
+int glisser_mlp_set_params(glisser_mlp_t *m, const float *params);   /* also resets the Adam state */
+
+/* Adam on the mean squared error of the normalised output: `steps`
+ * minibatches of `batch` (a multiple of 128) samples drawn with replacement
+ * from `seed`, learning rate cosine-decayed from lr to lr_min.  losses
+ * (optional, [steps]) receives each minibatch's loss. */
+int glisser_mlp_train(glisser_mlp_t *m, int steps, int batch, float lr, float lr_min, uint64_t seed, float *losses);
+/* Gradient of the mean loss over the n given samples, by the training
+ * kernels (grad [GLISSER_MLP_NPARAM]); loss = that mean loss. */
+int glisser_mlp_gradients(glisser_mlp_t *m, const float *feat, const float *target, size_t n, float *grad,
+                          float *loss);
+/* z for each feature triple by the drift's own inference routine (NaN
+ * outside the feature box). */
+int glisser_mlp_predict(glisser_mlp_t *m, const float *feat, size_t n, float *y);
+/* Weights file for glisser_set_starter / glisser_ensemble_set_starter. */
+int glisser_mlp_save(const glisser_mlp_t *m, const char *path);
+/* The current weights as the drift reads them (device pointer owned by m,
+ * valid until the next change of weights or normalisation). */
+int glisser_mlp_device_weights(glisser_mlp_t *m, const void **dev);
+
+/* One Kepler drift by dt of each device state [0, n) (r, v updated in place)
+ * with the time-block kernel's drift routine and the given starter (`mlp`:
+ * device weights for GLISSER_STARTER_LEARNED, else ignored); evals / flags
+ * (optional device arrays) receive each drift's Stumpff evaluations and
+ * flag bits (0x04 not converged, 0x08 unbound).  Asynchronous on `stream`. */
+int glisser_kepler_drift_states(const glisser_particles *pa, size_t n, double dt, double mu, int starter,
+                                const void *mlp, uint32_t *evals, uint16_t *flags, void *stream);
 
 #ifdef __cplusplus
 }

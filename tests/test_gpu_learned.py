@@ -1,0 +1,211 @@
+"""Learned Kepler starter on the GPU: training kernels against the CPU
+oracle, logged samples against exact solves, what the trained network saves,
+and that the starter never changes the accepted solution.
+
+Workload: the scattered-disk distribution (Sun + a Neptune-mass planet at
+30 au; a log-uniform in 30..1000 au, e up to 0.95, i up to 40 deg), dt = 180 d,
+Outer-Limit raised to 1e5 au.
+"""
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import glisser_gb300 as G  # noqa: E402
+from glisser_gb300 import learned as L  # noqa: E402
+from glisser_gb300 import synth  # noqa: E402
+from oracle import mlp_oracle as M  # noqa: E402
+
+CFG = ("Time-Step 180\nTime-Block-Size %d\nFinal-Time 1e30\nCull-Radius 0.5\nOuter-Limit 1e5\n"
+       "Input-File x\nOutput-Folder x\n")
+DT = 180.0
+
+
+@pytest.fixture(scope="module", autouse=True)
+def native():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    G.build()
+    G.lib()
+
+
+def simulation(n, seed, T=64, starter=G.STARTER_SERIES, mlp_path=None):
+    m, pr, pv, r, v = synth.cartesian_state(3, n, seed)
+    sim = G.Simulation(CFG % T)
+    sim.set_planets(m, pr, pv)
+    sim.set_particles(r, v)
+    sim.set_starter(starter, mlp_path)
+    sim.init()
+    return sim, (m, r, v)
+
+
+@pytest.fixture(scope="module")
+def trained(tmp_path_factory):
+    tr = L.Trainer(1 << 18, seed=5)
+    sim, state = simulation(8192, seed=11)
+    losses = L.train_on_simulation(sim, tr, blocks=16, steps=3000, batch=8192, lr=3e-3, lr_min=1e-5, seed=3)
+    path = str(tmp_path_factory.mktemp("mlp") / "starter.bin")
+    tr.save(path)
+    return tr, losses, state, path
+
+
+def features(r, v, mu, dt):
+    r0 = np.linalg.norm(r, axis=1)
+    u = (r * v).sum(1)
+    alpha = 2 * mu / r0 - (v * v).sum(1)
+    tau = dt * np.sqrt(mu / r0 ** 3)
+    return np.stack([np.log(tau), u / np.sqrt(mu * r0), alpha * r0 / mu], 1), r0, u, alpha
+
+
+def exact_s(dt, r0, u, mu, alpha, s):
+    """Newton on the universal Kepler equation with closed-form Stumpff
+    functions (float64), from a nearby start."""
+    for _ in range(30):
+        x = alpha * s * s
+        sx = np.sqrt(np.abs(x))
+        with np.errstate(invalid="ignore", divide="ignore"):
+            c2 = np.where(x > 0, (1 - np.cos(sx)) / x, (np.cosh(sx) - 1) / -x)
+            c3 = np.where(x > 0, (sx - np.sin(sx)) / sx ** 3, (np.sinh(sx) - sx) / sx ** 3)
+        small = np.abs(x) < 1e-3
+        c2 = np.where(small, 0.5 - x / 24 + x * x / 720, c2)
+        c3 = np.where(small, 1 / 6 - x / 120 + x * x / 5040, c3)
+        g1 = s * (1 - x * c3)
+        g2 = s * s * c2
+        g3 = s ** 3 * c3
+        f = r0 * g1 + u * g2 + mu * g3 - dt
+        fp = r0 * (1 - x * c2) + u * g1 + mu * g2
+        s = s - f / fp
+    return s
+
+
+def test_gradients_match_oracle():
+    rng = np.random.default_rng(4)
+    tr = L.Trainer(1024, seed=9)
+    norm = dict(in_mean=[-6.5, 0.0, 1.1], in_scale=[0.45, 2.2, 1.7], x_lo=[-30, -5, -1], x_hi=[5, 5, 5],
+                out_mean=0.002, out_scale=0.015)
+    tr.norm = norm
+    p = M.init_params(9)
+    p[M.OFF_B1:M.OFF_W2] = rng.normal(0, 0.2, 32)
+    p[M.OFF_B2:M.OFF_W3] = rng.normal(0, 0.2, 32)
+    tr.params = p
+    n = 1000                      # not a multiple of the 128-sample tile
+    feat = np.stack([rng.uniform(-10, 0, n), rng.uniform(-1, 1, n), rng.uniform(0, 2, n)], 1).astype(np.float32)
+    target = rng.normal(0.0, 0.03, n).astype(np.float32)
+    g_gpu, loss_gpu = tr.gradients(feat, target)
+    nm = tr.norm
+    loss, g = M.loss_and_grad(p, nm, feat.astype(np.float64), target.astype(np.float64))
+    assert abs(loss_gpu - loss) <= 1e-5 * loss
+    for a, b in ((M.OFF_W1, M.OFF_B1), (M.OFF_B1, M.OFF_W2), (M.OFF_W2, M.OFF_B2), (M.OFF_B2, M.OFF_W3),
+                 (M.OFF_W3, M.OFF_B3), (M.OFF_B3, M.NPARAM)):
+        d = np.linalg.norm(g_gpu[a:b] - g[a:b]) / np.linalg.norm(g[a:b])
+        assert d < 1e-4, (a, d)      # FP32 accumulation and fast exp against float64
+
+
+def test_logged_samples_are_plain_solves(trained):
+    tr, _, (m, r, v), _ = trained
+    mu = m[0]
+    n = len(r)
+    feat, z = tr.get_samples(0, n)           # first log: the initial states, in id order
+    f_ref, r0, u, alpha = features(r, v, mu, DT)
+    assert np.allclose(feat, f_ref, rtol=2e-6, atol=2e-6)
+    tau = np.exp(f_ref[:, 0])
+    s0 = DT / r0 * np.exp(z.astype(np.float64) * tau)
+    s = exact_s(DT, r0, u, mu, alpha, s0)
+    z_ref = np.log(s * r0 / DT) / tau
+    assert np.all(np.isfinite(z))
+    assert np.max(np.abs(z - z_ref) / (1e-3 + np.abs(z_ref))) < 1e-5
+    count, evals = tr.samples()
+    assert 15 * n < count <= 16 * n and evals > count
+
+
+def test_training_converges(trained):
+    _, losses, _, _ = trained
+    assert np.all(np.isfinite(losses))
+    assert losses[-200:].mean() < 1e-2 * losses[:10].mean()
+
+
+def test_inference_matches_oracle(trained):
+    tr, _, _, _ = trained
+    feat, _ = tr.get_samples(5 * 8192, 4096)
+    y_gpu = tr.predict(feat)
+    y_ref = M.predict(tr.params, tr.norm, feat.astype(np.float64))
+    ok = np.isfinite(y_ref)
+    assert np.array_equal(np.isfinite(y_gpu), ok)
+    scale = float(tr.norm["out_scale"])
+    assert np.max(np.abs(y_gpu[ok] - y_ref[ok])) < 3e-5 * scale + 1e-6
+
+
+def test_learned_starter_saves_newton_passes(trained):
+    tr, _, _, _ = trained
+    m, pr, pv, r, v = synth.cartesian_state(3, 8192, seed=12)     # held out
+    mu = m[0]
+    out = {}
+    for name, st in (("classic", G.STARTER_CLASSIC), ("learned", G.STARTER_LEARNED), ("series", G.STARTER_SERIES)):
+        out[name] = L.drift_states(r, v, DT, mu, st, tr)
+    ev = {k: o[2].mean() for k, o in out.items()}
+    print("mean Stumpff evaluations per drift:", ev)
+    assert ev["learned"] < ev["classic"] - 0.5
+    for k in ("learned", "series"):
+        assert np.array_equal(out[k][3], out["classic"][3])
+        rr = np.linalg.norm(out[k][0] - out["classic"][0], axis=1) / np.linalg.norm(out["classic"][0], axis=1)
+        assert rr.max() < 1e-12, (k, rr.max())
+
+
+def test_simulation_learned_matches_series(trained):
+    _, _, _, path = trained
+    runs = {}
+    for st in (G.STARTER_SERIES, G.STARTER_LEARNED):
+        sim, _ = simulation(2048, seed=13, T=256, starter=st, mlp_path=path if st == G.STARTER_LEARNED else None)
+        for _ in range(4):                    # 1024 steps
+            sim.loop()
+        p = sim.particles()
+        o = np.argsort(p["id"])
+        runs[st] = ({k: p[k][o] for k in ("r", "v", "flags", "id")}, sim.counts(), sim.stats())
+    a, b = runs[G.STARTER_SERIES], runs[G.STARTER_LEARNED]
+    assert np.array_equal(a[0]["flags"], b[0]["flags"])
+    assert a[1] == b[1]
+    live = a[0]["flags"] == 0
+    err = np.linalg.norm(a[0]["r"] - b[0]["r"], axis=1) / np.linalg.norm(a[0]["r"], axis=1)
+    assert err[live].max() < 1e-10, err[live].max()
+    assert a[2]["particle_steps"] == b[2]["particle_steps"]
+
+
+def test_ensemble_learned_matches_series_and_is_launch_invariant(trained):
+    _, _, _, path = trained
+    systems = []
+    for s in range(3):
+        m, pr, pv, r, v = synth.cartesian_state(3, [300, 900, 129][s], seed=20 + s)
+        systems.append((m, pr, pv, r, v))
+
+    def run(starter, cta=128, ppt=1, graph=True):
+        ens = G.Ensemble(CFG % 128, len(systems))
+        for s, (m, pr, pv, r, v) in enumerate(systems):
+            ens.set_system(s, m, pr, pv, r, v)
+        ens.set_starter(starter, path if starter == G.STARTER_LEARNED else None)
+        ens.set_shape(cta, ppt)
+        ens.set_graph(graph)
+        ens.init()
+        for _ in range(4):
+            ens.step()
+        return [ens.particles(s) for s in range(len(systems))]
+
+    ser = run(G.STARTER_SERIES)
+    lrn = run(G.STARTER_LEARNED)
+    lrn2 = run(G.STARTER_LEARNED, 64, 2, False)
+    for s in range(len(systems)):
+        assert np.array_equal(ser[s]["flags"], lrn[s]["flags"])
+        err = np.linalg.norm(ser[s]["r"] - lrn[s]["r"], axis=1) / np.linalg.norm(ser[s]["r"], axis=1)
+        assert err.max() < 1e-10
+        assert np.array_equal(lrn[s]["r"], lrn2[s]["r"])
+
+
+def test_bad_weights_file_is_rejected(tmp_path):
+    p = tmp_path / "bad.bin"
+    p.write_bytes(b"GLMLP000" + bytes(100))
+    sim = G.Simulation(CFG % 64)
+    with pytest.raises(G.GlisserError):
+        sim.set_starter(G.STARTER_LEARNED, str(p))
+    assert os.path.exists(p)
