@@ -385,6 +385,92 @@ def run_learned(G, args, rank, barrier):
     }
 
 
+def run_history(G, args, rank, barrier):
+    """Planetary history + encounter flagging: a history of the Sun +
+    Neptune-mass planet (yr units) written by the library's own planet-only
+    WH (dt 0.2 yr, one snapshot per 100 steps), then Neptune-crossing
+    particles (a~U(20,40) au, e~U(0,0.3), i~U(0,10deg)) integrated against it
+    with the history evaluated on the device each block and per-step
+    3-Hill-radius encounter flags handed off through the ballot-compacted
+    list.  Series and learned starters, the learned one trained on this
+    run's own logged solves."""
+    import tempfile
+    import torch
+    from glisser_gb300 import learned as L
+    from glisser_gb300 import synth
+    tmp = tempfile.mkdtemp()
+    hist = os.path.join(tmp, "plhist.out")
+    m, pr, pv, r, v = synth.cartesian_state(5, args.history_particles, seed=3000 + rank)
+    pre = G.Simulation("Time-Step 0.2\nTime-Block-Size 100\nFinal-Time 1e9\nLimit-Particle-Count 0\n"
+                       "Input-File unused\nOutput-Folder unused\n")
+    pre.set_planets(m, pr, pv)
+    pre.set_particles(np.zeros((0, 3)), np.zeros((0, 3)))
+    pre.init()
+    pre.write_plhist(hist, begin=True)
+    n_intervals = 4 * (1 + args.history_blocks) + args.learned_log_blocks + 8
+    for _ in range(n_intervals):
+        pre.loop()
+        pre.write_plhist(hist)
+    del pre
+    cfg = ("Time-Step 0.2\nTime-Block-Size 100\nFinal-Time 1e9\nRead-Planet-History 1\nPlanet-History-File %s\n"
+           "Encounter-RH-Factor 3\nCull-Radius 0.5\nOuter-Limit 300\nInput-File unused\nOutput-Folder unused\n"
+           % hist)
+
+    def make(starter, path=None):
+        sim = G.Simulation(cfg)
+        sim.set_planets(m, pr, pv)
+        sim.set_particles(r, v)
+        sim.set_starter(starter, path)
+        sim.init()
+        return sim
+
+    tr = L.Trainer(args.history_particles * args.learned_log_blocks + 1, seed=9)
+    sim = make(G.STARTER_SERIES)
+    for _ in range(args.learned_log_blocks):
+        tr.log_simulation(sim)
+        sim.loop()
+    del sim
+    tr.fit_norm()
+    losses = tr.train(args.learned_train_steps, batch=16384, lr=3e-3, lr_min=1e-5, seed=17)
+    path = os.path.join(tmp, "starter.bin")
+    tr.save(path)
+
+    legs = {}
+    for name, st in (("series", G.STARTER_SERIES), ("learned", G.STARTER_LEARNED)):
+        sim = make(st, path if st == G.STARTER_LEARNED else None)
+        stream = torch.cuda.ExternalStream(sim.stream())
+        sim.loop()                                   # warm-up block
+        barrier()
+        s0 = sim.stats()
+        alive0 = sim.counts()["n_alive"]
+        flagged = 0
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        kms = 0.0
+        for _ in range(args.history_blocks):
+            kms += sim.loop()[2]
+            flagged += len(sim.flagged()["id"])
+        e1.record(stream)
+        e1.synchronize()
+        el = e0.elapsed_time(e1) * 1e-3
+        s1 = sim.stats()
+        ps = s1["particle_steps"] - s0["particle_steps"]
+        legs[name] = {"value": ps / el, "unit": UNIT, "kernel_ms_per_block": kms / args.history_blocks,
+                      "kepler_evals_per_particle_step": (s1["kepler_evals"] - s0["kepler_evals"]) / max(ps, 1),
+                      "alive_start": alive0, "alive_end": sim.counts()["n_alive"], "handed_off": flagged,
+                      "launches_per_block": (s1["launches"] - s0["launches"]) / args.history_blocks}
+        del sim
+    return {
+        "workload": "history-encounters: planetary history of Sun + Neptune-mass planet (a=30 au, yr units) from the "
+                    "library's planet-only WH, dt=0.2 yr, one snapshot per 100 steps, evaluated on the device; %d "
+                    "particles a~U(20,40) au e~U(0,0.3) i~U(0,10deg); Encounter-RH-Factor 3, Time-Block-Size 100"
+                    % args.history_particles,
+        "blocks": args.history_blocks, "starters": legs,
+        "training": {"samples": tr.samples()[0], "loss_last": float(losses[-100:].mean())},
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -404,6 +490,9 @@ def main():
     ap.add_argument("--learned-log-blocks", type=int, default=10)
     ap.add_argument("--learned-train-steps", type=int, default=8000)
     ap.add_argument("--learned-blocks", type=int, default=3)
+    ap.add_argument("--no-history", action="store_true")
+    ap.add_argument("--history-particles", type=int, default=2_000_000)
+    ap.add_argument("--history-blocks", type=int, default=20)
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -534,6 +623,9 @@ def main():
     learned = None
     if not args.no_learned:
         learned = run_learned(G, args, rank, barrier)
+    history = None
+    if not args.no_history:
+        history = run_history(G, args, rank, barrier)
 
     if rank == 0:
         line = {
@@ -561,6 +653,7 @@ def main():
             "cpu_baseline": cpu,
             "ensembles": ensembles,
             "learned": learned,
+            "history": history,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

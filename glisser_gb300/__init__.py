@@ -101,6 +101,7 @@ def lib():
             "glisser_set_particles": ([P, C.c_size_t, D, D, U32, U16, D], C.c_int),
             "glisser_set_starter": ([P, C.c_int, C.c_char_p], C.c_int),
             "glisser_init": ([P], C.c_int),
+            "glisser_set_device_interp": ([P, C.c_int], C.c_int),
             "glisser_step_block": ([P, C.POINTER(C.c_int), D, D], C.c_int),
             "glisser_run": ([P, C.c_int], C.c_int),
             "glisser_finish": ([P], C.c_int),
@@ -282,6 +283,10 @@ class Simulation:
 
     def set_starter(self, starter, mlp_path=None):
         self._check(lib().glisser_set_starter(self.h, starter, mlp_path.encode() if mlp_path else None))
+
+    def set_device_interp(self, on=True):
+        """Planetary history per step on the device (default) or the host; before init."""
+        self._check(lib().glisser_set_device_interp(self.h, int(bool(on))))
 
     def init(self):
         self._check(lib().glisser_init(self.h))

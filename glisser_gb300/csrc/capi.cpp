@@ -221,6 +221,16 @@ int glisser_set_starter(glisser_t* h, int starter, const char* mlp_path)
     });
 }
 
+int glisser_set_device_interp(glisser_t* h, int on)
+{
+    return guarded(h, [&] {
+        glisser::Executor& ex = exec_of(h);
+        if (ex.initialized()) throw std::invalid_argument("glisser_set_device_interp: call before init");
+        ex.set_device_interp(on != 0);
+        return GLISSER_OK;
+    });
+}
+
 int glisser_init(glisser_t* h)
 {
     return guarded(h, [&] {

@@ -15,6 +15,7 @@
 // The full particle state comes back to the host mirror only when someone
 // reads it (outputs, the C ABI), not every block.
 #include "executor.h"
+#include "interp.h"
 
 #include <algorithm>
 #include <chrono>
@@ -92,6 +93,11 @@ struct Executor::Impl {
     double* h_rh[2] = { nullptr, nullptr };
     uint32_t* h_id[2] = { nullptr, nullptr };
     uint32_t blk_npl[2] = { 0, 0 }, blk_len[2] = { 0, 0 };
+    // device interpolation of the planetary history: element tracks per
+    // buffer; log_on_device[b] = the host copy of log b is not filled
+    InterpTrack* d_tracks[2] = { nullptr, nullptr };
+    InterpTrack* h_tracks[2] = { nullptr, nullptr };
+    bool log_on_device[2] = { false, false };
     int blk = 1;   // planet buffer the next kernel uses (the first block fills 0)
     // hand-off and counters
     uint32_t* d_ctr = nullptr;            // [0] count [1] status [2] n0 [3] n1
@@ -117,7 +123,8 @@ struct Executor::Impl {
         if (!device) return;   // nothing was allocated on the device
         for (int b = 0; b < 2; b++) {
             buf[b].release();
-            cudaFree(d_log[b]); cudaFree(d_m[b]); cudaFree(d_rh[b]); cudaFree(d_id[b]);
+            cudaFree(d_log[b]); cudaFree(d_m[b]); cudaFree(d_rh[b]); cudaFree(d_id[b]); cudaFree(d_tracks[b]);
+            cudaFreeHost(h_tracks[b]);
             if (device) {
                 cudaFreeHost(h_log[b]); cudaFreeHost(h_m[b]); cudaFreeHost(h_rh[b]); cudaFreeHost(h_id[b]);
             }
@@ -351,20 +358,60 @@ void Executor::update_planets()
         cur_tbsize_ = std::min<size_t>(cfg.tbsize, ip.n_ts - ip.cur_ts);
         npl = (uint32_t)(ip.n_alive + 1);
         if (npl > d.max_npl) throw StateError("planetary history has more planets than the device buffers hold");
-        // positions into the log records (after the h0 slot), then h0
-        ip.fill(pl_, cur_tbsize_, ip.rel_t, cur_dt_, log + 3, 3 * (size_t)npl);
+        if (d.device && device_interp_) {
+            // the device evaluates every step's record (interp.cu); the host
+            // keeps the interval bookkeeping and the live planets, which end
+            // at the block's last step time (accumulated as the per-step
+            // fill accumulates it)
+            for (size_t j = 0; j < ip.n_alive; j++) {
+                pl_.id[j + 1] = ip.ids[j];
+                pl_.m[j + 1] = ip.mass[j];
+                InterpTrack& q = d.h_tracks[nb][j];
+                const Vec3* src[4] = { &ip.aei_i[j], &ip.daei[j], &ip.oom_i[j], &ip.doom[j] };
+                double* dst[4] = { q.aei_i, q.daei, q.oom_i, q.doom };
+                for (int c = 0; c < 4; c++) {
+                    dst[c][0] = src[c]->x;
+                    dst[c][1] = src[c]->y;
+                    dst[c][2] = src[c]->z;
+                }
+                q.m = ip.mass[j];
+                q.pad = 0;
+            }
+            double tt = ip.rel_t + cur_dt_, last = tt;
+            for (size_t k = 0; k < cur_tbsize_; k++) {
+                if (tt > ip.t1 - ip.t0 + 1e-8)
+                    throw std::runtime_error("interpolation ran too long, timechunk exceeded lookup boundary");
+                last = tt;
+                tt += cur_dt_;
+            }
+            if (cur_tbsize_ > 0) {
+                pl_.r[0] = pl_.v[0] = Vec3{ 0, 0, 0 };
+                ip.fill_one(pl_, last);
+            }
+            ck(cudaMemcpyAsync(d.d_tracks[nb], d.h_tracks[nb], ip.n_alive * sizeof(InterpTrack),
+                               cudaMemcpyHostToDevice, d.htd), "upload tracks");
+            ck(launch_interp_fill(d.d_tracks[nb], npl - 1, (uint32_t)cur_tbsize_, ip.rel_t, cur_dt_, d.d_log[nb],
+                                  d.htd), "interpolation kernel");
+            launches_total_ += 1;
+            d.log_on_device[nb] = true;
+        } else {
+            // positions into the log records (after the h0 slot), then h0
+            ip.fill(pl_, cur_tbsize_, ip.rel_t, cur_dt_, log + 3, 3 * (size_t)npl);
+            for (size_t s = 0; s < cur_tbsize_; s++) {
+                double* rec = log + s * 3 * npl;
+                Vec3 h0 = indirect_term(rec + 3, pl_.m, npl);
+                rec[0] = h0.x; rec[1] = h0.y; rec[2] = h0.z;
+            }
+            d.log_on_device[nb] = false;
+        }
         pl_.n_alive = npl;
         ip.rel_t += (double)cur_tbsize_ * cur_dt_;
         ip.cur_ts += cur_tbsize_;
-        for (size_t s = 0; s < cur_tbsize_; s++) {
-            double* rec = log + s * 3 * npl;
-            Vec3 h0 = indirect_term(rec + 3, pl_.m, npl);
-            rec[0] = h0.x; rec[1] = h0.y; rec[2] = h0.z;
-        }
     } else {
         cur_dt_ = cfg.dt;
         cur_tbsize_ = cfg.tbsize;
         npl = (uint32_t)pl_.n_alive;
+        d.log_on_device[nb] = false;
         for (size_t s = 0; s < cur_tbsize_; s++) {
             Vec3 h0 = integ_.step(pl_, cur_dt_);
             double* rec = log + s * 3 * npl;
@@ -386,7 +433,9 @@ void Executor::update_planets()
     d.blk = nb;
     if (!d.device) return;
     size_t recs = (cur_tbsize_ + 1) & ~(size_t)1;
-    ck(cudaMemcpyAsync(d.d_log[nb], log, recs * 3 * npl * sizeof(double), cudaMemcpyHostToDevice, d.htd), "upload log");
+    if (!d.log_on_device[nb])
+        ck(cudaMemcpyAsync(d.d_log[nb], log, recs * 3 * npl * sizeof(double), cudaMemcpyHostToDevice, d.htd),
+           "upload log");
     ck(cudaMemcpyAsync(d.d_m[nb], d.h_m[nb], npl * sizeof(double), cudaMemcpyHostToDevice, d.htd), "upload m");
     ck(cudaMemcpyAsync(d.d_id[nb], d.h_id[nb], npl * sizeof(uint32_t), cudaMemcpyHostToDevice, d.htd), "upload ids");
     ck(cudaMemcpyAsync(d.d_rh[nb], d.h_rh[nb], npl * sizeof(double), cudaMemcpyHostToDevice, d.htd), "upload rh");
@@ -396,10 +445,15 @@ void Executor::update_planets()
 void Executor::planet_block(std::vector<double>& log, std::vector<double>& m, std::vector<uint32_t>& id,
                             std::vector<double>& rh, uint32_t& npl, uint32_t& len) const
 {
-    const Impl& d = *d_;
+    Impl& d = *d_;
     int b = d.blk;
     npl = d.blk_npl[b];
     len = d.blk_len[b];
+    if (d.log_on_device[b] && len > 0) {
+        ck(cudaEventSynchronize(d.uploaded[b]), "interpolation");
+        ck(cudaMemcpy(d.h_log[b], d.d_log[b], (size_t)len * 3 * npl * sizeof(double), cudaMemcpyDeviceToHost),
+           "download log");
+    }
     log.assign(d.h_log[b], d.h_log[b] + (size_t)len * 3 * npl);
     m.assign(d.h_m[b], d.h_m[b] + npl);
     rh.assign(d.h_rh[b], d.h_rh[b] + npl);
@@ -524,6 +578,8 @@ void Executor::init()
         ck(cudaMallocHost(&d.h_m[b], d.max_npl * sizeof(double)), "pinned");
         ck(cudaMallocHost(&d.h_rh[b], d.max_npl * sizeof(double)), "pinned");
         ck(cudaMallocHost(&d.h_id[b], d.max_npl * sizeof(uint32_t)), "pinned");
+        ck(cudaMalloc(&d.d_tracks[b], d.max_npl * sizeof(InterpTrack)), "cudaMalloc tracks");
+        ck(cudaMallocHost(&d.h_tracks[b], d.max_npl * sizeof(InterpTrack)), "pinned");
     }
     size_t cap = std::max<size_t>(n, 1);
     ck(cudaMalloc(&d.d_ctr, 16 * sizeof(uint32_t)), "cudaMalloc counters");

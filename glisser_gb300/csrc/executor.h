@@ -61,6 +61,9 @@ public:
 
     // Kepler starter selection (GLISSER_STARTER_*) and learned weights blob
     void set_starter(int starter, const std::vector<uint8_t>* mlp_blob);
+    // Planetary history evaluated per step on the device (default) or on the
+    // host (the reference's arrangement); set before init.
+    void set_device_interp(bool on) { device_interp_ = on; }
     unsigned long long kepler_evals() const { return evals_total_; }
     unsigned long long particle_steps() const { return psteps_total_; }
     unsigned long long launches() const { return launches_total_; }
@@ -86,6 +89,7 @@ private:
     size_t cur_tbsize_ = 0, prev_tbsize_ = 0;
     bool starting_interval_ = false;
     int starter_ = GLISSER_STARTER_SERIES;
+    bool device_interp_ = true;
     unsigned long long evals_total_ = 0;
     unsigned long long psteps_total_ = 0;
     unsigned long long launches_total_ = 0;

@@ -40,7 +40,14 @@ def _deps():
     return max(os.path.getmtime(h) for h in hdrs)
 
 
+# Translation units that must not contract a*b+c into FMA: the device
+# interpolation of the planetary history evaluates the host interpolator's
+# formulas and is compared with it.
+PER_FILE_FLAGS = {"interp.cu": ("--fmad=false",)}
+
+
 def _compile(src, extra_flags=()):
+    extra_flags = tuple(extra_flags) + PER_FILE_FLAGS.get(os.path.basename(src), ())
     obj = os.path.join(OUT, os.path.basename(src) + ".o")
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(src), _deps()):
         return obj

@@ -184,6 +184,11 @@ int glisser_set_particles(glisser_t *h, size_t n, const double *r, const double 
                           const uint16_t *flags, const double *deathtime);
 
 /* Executor::init (src/executor.cu:85-217). */
+/* With Read-Planet-History: evaluate the planetary history for every step
+ * of a block on the device (on = 1, the default) or on the host (on = 0, the
+ * reference's arrangement, src/interp.cpp:113-165).  Call before init. */
+int glisser_set_device_interp(glisser_t *h, int on);
+
 int glisser_init(glisser_t *h);
 /* Executor::loop (src/executor.cu:598-764): one time block.  *safe_to_output
  * mirrors loop's return value. */

@@ -18,8 +18,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 from glisser_gb300 import synth  # noqa: E402
+from glisser_gb300.metrics import jacobi_constant  # noqa: E402
 
 REF_LIB = os.path.join(ROOT, "oracle", "_ref", "libglisser_ref.so")
+REFERENCE = os.environ.get("GLISSER_REF_DIR", "/root/reference")
 D = C.POINTER(C.c_double)
 U32 = C.POINTER(C.c_uint32)
 U16 = C.POINTER(C.c_uint16)
@@ -161,6 +163,44 @@ def run_case(L, tmp, name, config_lines, pl_m, pl_r, pl_v, r, v, nblocks, out):
     np.savez_compressed(os.path.join(HERE, out), **rec)
     print("wrote", out, "alive after each block:", [int(rec["out%d_n_alive" % b]) for b in range(nblocks)])
     return run
+
+
+def gen_threebody(L):
+    """The reference's own restricted three-body example
+    (example/threebody-particles/state.in.full: 1000 particles; Sun, a
+    massless body at 5.2 au and a 2.04e-3 primary at 30.4 au, yr units) run by
+    the reference for 50 blocks of 100 steps of 0.2 yr (1000 yr) with
+    Encounter-RH-Factor 3.5, as in example/threebody-particles/config.in."""
+    state = os.path.join(REFERENCE, "example", "threebody-particles", "state.in.full")
+    lines = ["Time-Step 0.2", "Time-Block-Size 100", "Final-Time 1000", "Encounter-RH-Factor 3.5",
+             "Cull-Radius 0.5"]
+    cfg = "\n".join(lines + ["Input-File " + state, "Output-Folder /tmp"]) + "\n"
+    run = RefRun(L, cfg)
+    pm, pr, pv, pid = run.planets()
+    p0 = run.particles()
+    rec = dict(pl_m=pm, pl_r=pr, pl_v=pv, pl_id=pid, r0=p0["r"], v0=p0["v"], id0=p0["id"], flags0=p0["flags"],
+               config=np.array("\n".join(lines)))
+    o = np.argsort(p0["id"])
+    c0 = jacobi_constant(pm, pr, pv, p0["r"][o], p0["v"][o])
+    maxerr = np.zeros(len(o))
+    for b in range(50):
+        run.loop()
+        st = run.particles()
+        m_, r_, v_, _ = run.planets()
+        o = np.argsort(st["id"])
+        c = jacobi_constant(m_, r_, v_, st["r"][o], st["v"][o])
+        live = st["flags"][o] == 0
+        maxerr = np.where(live, np.maximum(maxerr, np.abs(c - c0) / np.abs(c0)), maxerr)
+        if b in (4, 49):
+            for k in ("r", "v", "id", "flags", "dti"):
+                rec["out%d_%s" % (b, k)] = st[k]
+            rec["out%d_n_alive" % b] = np.array(run.counts()[1])
+    rec["cj0"] = c0
+    rec["cj_maxerr"] = maxerr
+    np.savez_compressed(os.path.join(HERE, "threebody_t100.npz"), **rec)
+    live = rec["out49_flags"] == 0
+    print("wrote threebody_t100.npz: alive after 5 / 50 blocks", int(rec["out4_n_alive"]), int(rec["out49_n_alive"]),
+          "max C_J error (alive)", maxerr[np.sort(rec["out49_id"][live])].max())
 
 
 def main():
@@ -323,4 +363,8 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["threebody"]:
+        gen_threebody(ref())
+    else:
+        main()
+        gen_threebody(ref())

@@ -100,3 +100,33 @@ def test_quirk_switch_changes_only_flagged_starts():
     b = exec_for(d, cfg, ref_quirks=False)
     pa, pb = a.particles(), b.particles()
     assert not np.array_equal(pa["a"], pb["a"])
+
+
+def test_threebody_example_matches_reference():
+    """The reference's restricted three-body example (1000 particles, 1000 yr,
+    Encounter-RH-Factor 3.5): the oracle reproduces the reference's flags and
+    survivors bit for bit, its states, and its Jacobi-constant drift."""
+    from glisser_gb300.metrics import jacobi_constant
+    g = np.load(os.path.join(GOLD, "threebody_t100.npz"))
+    ex = O.Exec(g["pl_m"], g["pl_r"], g["pl_v"], g["pl_id"], g["r0"], g["v0"], g["id0"], g["flags0"], dt=0.2,
+                tbsize=100, outer_r=300.0, cull_r=0.5, esf=3.5)
+    o = np.argsort(g["id0"])
+    c0 = jacobi_constant(g["pl_m"], g["pl_r"], g["pl_v"], g["r0"][o], g["v0"][o])
+    assert np.array_equal(c0, g["cj0"])
+    maxerr = np.zeros(len(o))
+    for b in range(50):
+        ex.loop()
+        p = ex.particles()
+        pl = ex.planets()
+        o = np.argsort(p["id"])
+        c = jacobi_constant(pl["m"], pl["r"], pl["v"], p["r"][o], p["v"][o])
+        live = p["flags"][o] == 0
+        maxerr = np.where(live, np.maximum(maxerr, np.abs(c - c0) / np.abs(c0)), maxerr)
+        if b in (4, 49):
+            assert np.array_equal(p["id"], g["out%d_id" % b])
+            assert np.array_equal(p["flags"], g["out%d_flags" % b])
+            assert np.array_equal(p["dti"], g["out%d_dti" % b])
+            assert np.allclose(p["r"], g["out%d_r" % b], rtol=1e-12, atol=0)
+    live = g["out49_flags"][np.argsort(g["out49_id"])] == 0
+    assert np.allclose(maxerr[live], g["cj_maxerr"][live], rtol=1e-6, atol=1e-15)
+    assert g["cj_maxerr"][live].max() < 1e-7
