@@ -471,6 +471,34 @@ def run_history(G, args, rank, barrier):
     }
 
 
+def run_track(G, sim):
+    """Track snapshot of the current state (alive particles by id, FP64
+    elements, float32 records): device writer vs the host writer, wall time
+    of the whole call including the file write."""
+    import tempfile
+    d = "/dev/shm" if os.path.isdir("/dev/shm") else tempfile.gettempdir()
+    path = os.path.join(d, "glisser_track_%d.out" % os.getpid())
+    try:
+        sim.write_track(path)                       # first call allocates the device buffers
+        t0 = time.perf_counter()
+        for _ in range(3):
+            sim.write_track(path)
+        dev_s = (time.perf_counter() - t0) / 3
+        size = os.path.getsize(path)
+        sim.set_device_output(False)
+        t0 = time.perf_counter()
+        sim.write_track(path)
+        host_s = time.perf_counter() - t0
+        sim.set_device_output(True)
+    finally:
+        if os.path.exists(path):
+            os.remove(path)
+    n = sim.counts()["n_alive"]
+    return {"particles": n, "bytes": size, "device_ms": dev_s * 1e3, "host_ms": host_s * 1e3,
+            "device_GBps": size / dev_s / 1e9, "host_GBps": size / host_s / 1e9,
+            "note": "wall time of glisser_write_track (kernels + device-to-host copy + file write to %s)" % d}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -491,6 +519,7 @@ def main():
     ap.add_argument("--learned-train-steps", type=int, default=8000)
     ap.add_argument("--learned-blocks", type=int, default=3)
     ap.add_argument("--no-history", action="store_true")
+    ap.add_argument("--no-track", action="store_true")
     ap.add_argument("--history-particles", type=int, default=2_000_000)
     ap.add_argument("--history-blocks", type=int, default=20)
     args = ap.parse_args()
@@ -616,6 +645,9 @@ def main():
                "sample": "%d particles x %d steps (%.1f s), oracle restatement of MVSKernel::step_forward "
                          "(src/wh.cu:113-177) on %d host threads" % (n_s, args.sample_steps, el, threads)}
 
+    track = None
+    if rank == 0 and not args.no_track:
+        track = run_track(G, sim)
     del sim
     ensembles = None
     if not args.no_ensembles:
@@ -654,6 +686,7 @@ def main():
             "ensembles": ensembles,
             "learned": learned,
             "history": history,
+            "track": track,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -102,6 +102,7 @@ def lib():
             "glisser_set_starter": ([P, C.c_int, C.c_char_p], C.c_int),
             "glisser_init": ([P], C.c_int),
             "glisser_set_device_interp": ([P, C.c_int], C.c_int),
+            "glisser_set_device_output": ([P, C.c_int], C.c_int),
             "glisser_step_block": ([P, C.POINTER(C.c_int), D, D], C.c_int),
             "glisser_run": ([P, C.c_int], C.c_int),
             "glisser_finish": ([P], C.c_int),
@@ -287,6 +288,10 @@ class Simulation:
     def set_device_interp(self, on=True):
         """Planetary history per step on the device (default) or the host; before init."""
         self._check(lib().glisser_set_device_interp(self.h, int(bool(on))))
+
+    def set_device_output(self, on=True):
+        """Track snapshots built on the device (default) or by the host writer."""
+        self._check(lib().glisser_set_device_output(self.h, int(bool(on))))
 
     def init(self):
         self._check(lib().glisser_init(self.h))

@@ -231,6 +231,14 @@ int glisser_set_device_interp(glisser_t* h, int on)
     });
 }
 
+int glisser_set_device_output(glisser_t* h, int on)
+{
+    return guarded(h, [&] {
+        exec_of(h).set_device_output(on != 0);
+        return GLISSER_OK;
+    });
+}
+
 int glisser_init(glisser_t* h)
 {
     return guarded(h, [&] {
@@ -386,6 +394,7 @@ int glisser_write_track(const glisser_t* h, const char* path, int append)
         glisser::Executor& ex = exec_of(hh);
         std::ofstream out(path, append ? (std::ios::binary | std::ios::app) : std::ios::binary);
         if (!out) throw glisser::IoError(std::string("cannot write ") + path);
+        if (ex.write_track_device(out)) return GLISSER_OK;
         const glisser::Particles& pa = ex.particles();
         size_t na = ex.initialized() ? ex.n_alive_host() : pa.n;
         std::vector<size_t> order(na);

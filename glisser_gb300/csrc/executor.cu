@@ -16,6 +16,7 @@
 // reads it (outputs, the C ABI), not every block.
 #include "executor.h"
 #include "interp.h"
+#include "track.h"
 
 #include <algorithm>
 #include <chrono>
@@ -98,6 +99,10 @@ struct Executor::Impl {
     InterpTrack* d_tracks[2] = { nullptr, nullptr };
     InterpTrack* h_tracks[2] = { nullptr, nullptr };
     bool log_on_device[2] = { false, false };
+    // device track writer: bitmap/scan scratch, record staging, pinned copy
+    uint32_t* d_track_scratch = nullptr;
+    void* d_track_out = nullptr;
+    void* h_track = nullptr;
     int blk = 1;   // planet buffer the next kernel uses (the first block fills 0)
     // hand-off and counters
     uint32_t* d_ctr = nullptr;            // [0] count [1] status [2] n0 [3] n1
@@ -135,6 +140,7 @@ struct Executor::Impl {
         cudaFreeHost(h_ctr); cudaFreeHost(h_evals); cudaFreeHost(h_ho_id); cudaFreeHost(h_ho_dti);
         cudaFreeHost(h_ho_flags); cudaFreeHost(h_dl); cudaFreeHost(h_dl_u32); cudaFreeHost(h_dl_flags);
         if (d_mlp) mlp_free(d_mlp);
+        cudaFree(d_track_scratch); cudaFree(d_track_out); cudaFreeHost(h_track);
         if (start) cudaEventDestroy(start);
         if (stop) cudaEventDestroy(stop);
         if (done) cudaEventDestroy(done);
@@ -147,6 +153,42 @@ Executor::Executor(const Config& c) : cfg(c), d_(new Impl()) {}
 Executor::~Executor() = default;
 
 void* Executor::stream() const { return d_->main; }
+
+bool Executor::write_track_device(std::ostream& out, double* ms)
+{
+    Impl& d = *d_;
+    if (!initialized_ || !d.device || !device_output_) return false;
+    const size_t n = n_alive_host();
+    if (max_id_ >= 0xFFFFFFE0u || (size_t)max_id_ > 4 * pa_.n + 4096) return false;   // sparse ids: host writer
+    if (!d.d_track_out) {
+        ck(cudaMalloc(&d.d_track_scratch, track_scratch_words(max_id_) * sizeof(uint32_t)), "cudaMalloc track scratch");
+        ck(cudaMalloc(&d.d_track_out, std::max<size_t>(pa_.n, 1) * 28), "cudaMalloc track records");
+        ck(cudaMallocHost(&d.h_track, std::max<size_t>(pa_.n, 1) * 28), "pinned track records");
+    }
+    const Planets& pl = snapshot_;
+    double cm;
+    Vec3 cr, cv;
+    track_particle_frame(pl, cfg.write_bary_track, cm, cr, cv);
+    TrackFrame fr{ cm, { cr.x, cr.y, cr.z }, { cv.x, cv.y, cv.z } };
+    ck(cudaEventRecord(d.start, d.main), "event");
+    ck(launch_track_records(&d.buf[d.cur].p, (uint32_t)n, max_id_, fr, d.d_track_scratch, d.d_track_out, d.main),
+       "track kernels");
+    launches_total_ += 4;
+    ck(cudaMemcpyAsync(d.h_track, d.d_track_out, n * 28, cudaMemcpyDeviceToHost, d.main), "track download");
+    ck(cudaEventRecord(d.stop, d.main), "event");
+    ck(cudaEventSynchronize(d.stop), "track");
+    if (ms) {
+        float f = 0;
+        ck(cudaEventElapsedTime(&f, d.start, d.stop), "elapsed");
+        *ms = f;
+    }
+    write_track_planets(out, pl, t, cfg.write_bary_track);
+    uint64_t cnt = n;
+    out.write(reinterpret_cast<const char*>(&cnt), sizeof cnt);
+    out.write(static_cast<const char*>(d.h_track), (std::streamsize)(n * 28));
+    out.flush();
+    return true;
+}
 
 void Executor::device_view(glisser_particles* pa, size_t* n, double* dt, double* mu) const
 {
@@ -534,6 +576,8 @@ void Executor::init()
     }
     (void)n_unflagged;
 
+    max_id_ = 0;
+    for (size_t k = 0; k < pa_.n; k++) max_id_ = std::max(max_id_, pa_.id[k]);
     d.max_npl = (uint32_t)std::min<size_t>(pl_.n, MAX_PLANETS);
     if (pl_.n > (size_t)MAX_PLANETS) throw StateError("more than 64 planets");
     d.log_cap = (cfg.tbsize + 1u) & ~1u;

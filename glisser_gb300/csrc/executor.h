@@ -64,6 +64,12 @@ public:
     // Planetary history evaluated per step on the device (default) or on the
     // host (the reference's arrangement); set before init.
     void set_device_interp(bool on) { device_interp_ = on; }
+    // Track snapshots built on the device (default) or by the host writer.
+    void set_device_output(bool on) { device_output_ = on; }
+    // Writes a track snapshot with the particle records built on the device
+    // (ms: kernels + download); false when that path does not apply (not
+    // initialised, no device particles, sparse ids, or switched off).
+    bool write_track_device(std::ostream& out, double* ms = nullptr);
     unsigned long long kepler_evals() const { return evals_total_; }
     unsigned long long particle_steps() const { return psteps_total_; }
     unsigned long long launches() const { return launches_total_; }
@@ -90,6 +96,8 @@ private:
     bool starting_interval_ = false;
     int starter_ = GLISSER_STARTER_SERIES;
     bool device_interp_ = true;
+    bool device_output_ = true;
+    uint32_t max_id_ = 0;
     unsigned long long evals_total_ = 0;
     unsigned long long psteps_total_ = 0;
     unsigned long long launches_total_ = 0;

@@ -225,8 +225,7 @@ void save_state(const Config& cfg, const Planets& pl, const Particles& pa, const
     }
 }
 
-void write_track(std::ostream& out, const Planets& pl, const Particles& pa, const std::vector<size_t>& order,
-                 double time, bool barycentric)
+void write_track_planets(std::ostream& out, const Planets& pl, double time, bool barycentric)
 {
     put<double>(out, time);
     put<uint64_t>(out, pl.n_alive > 0 ? pl.n_alive - 1 : 0);
@@ -248,9 +247,13 @@ void write_track(std::ostream& out, const Planets& pl, const Particles& pa, cons
         put<float>(out, (float)el.a); put<float>(out, (float)el.e); put<float>(out, (float)el.i);
         put<float>(out, (float)el.capom); put<float>(out, (float)el.om); put<float>(out, (float)el.f);
     }
-    put<uint64_t>(out, order.size());
-    double cm = pl.m[0];
-    Vec3 cr = pl.r[0], cv = pl.v[0];
+}
+
+void track_particle_frame(const Planets& pl, bool barycentric, double& cm, Vec3& cr, Vec3& cv)
+{
+    cm = pl.m[0];
+    cr = pl.r[0];
+    cv = pl.v[0];
     if (barycentric) {
         Vec3 rs{ 0, 0, 0 }, vs{ 0, 0, 0 };
         cm = 0;
@@ -262,6 +265,16 @@ void write_track(std::ostream& out, const Planets& pl, const Particles& pa, cons
         cr = rs / cm;
         cv = vs / cm;
     }
+}
+
+void write_track(std::ostream& out, const Planets& pl, const Particles& pa, const std::vector<size_t>& order,
+                 double time, bool barycentric)
+{
+    write_track_planets(out, pl, time, barycentric);
+    put<uint64_t>(out, order.size());
+    double cm;
+    Vec3 cr, cv;
+    track_particle_frame(pl, barycentric, cm, cr, cv);
     for (size_t k : order) {
         Elements el = to_elements(cm, pa.r[k] - cr, pa.v[k] - cv);
         put<uint32_t>(out, pa.id[k]);

@@ -43,6 +43,10 @@ void save_state_binary(std::ostream& out, const Config& cfg, const Planets& pl, 
 
 // save_binary_track (src/data.cpp:718-815) with elements; `order` lists the
 // particles to write (sorted by id by the caller).
+// Planet part of a track snapshot (time, planet count, planet records) and
+// the centre particle elements are taken about.
+void write_track_planets(std::ostream& out, const Planets& pl, double time, bool barycentric);
+void track_particle_frame(const Planets& pl, bool barycentric, double& cm, Vec3& cr, Vec3& cv);
 void write_track(std::ostream& out, const Planets& pl, const Particles& pa, const std::vector<size_t>& order,
                  double time, bool barycentric);
 

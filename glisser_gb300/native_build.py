@@ -41,9 +41,9 @@ def _deps():
 
 
 # Translation units that must not contract a*b+c into FMA: the device
-# interpolation of the planetary history evaluates the host interpolator's
-# formulas and is compared with it.
-PER_FILE_FLAGS = {"interp.cu": ("--fmad=false",)}
+# interpolation of the planetary history and the device track writer
+# evaluate the host restatement's formulas and are compared with it.
+PER_FILE_FLAGS = {"interp.cu": ("--fmad=false",), "track.cu": ("--fmad=false",)}
 
 
 def _compile(src, extra_flags=()):

@@ -189,6 +189,14 @@ int glisser_set_particles(glisser_t *h, size_t n, const double *r, const double 
  * reference's arrangement, src/interp.cpp:113-165).  Call before init. */
 int glisser_set_device_interp(glisser_t *h, int on);
 
+/* Track snapshots (glisser_write_track) with the particle records built on
+ * the device -- elements, float32 packing and id order in kernels, one
+ * device-to-host copy -- (on = 1, the default) or by the host writer (on =
+ * 0).  The device path applies when the particle ids are dense (largest id
+ * at most 4 n + 4096); otherwise the host writer runs.  Same file layout
+ * either way (src/data.cpp:718-815). */
+int glisser_set_device_output(glisser_t *h, int on);
+
 int glisser_init(glisser_t *h);
 /* Executor::loop (src/executor.cu:598-764): one time block.  *safe_to_output
  * mirrors loop's return value. */
