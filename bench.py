@@ -247,9 +247,13 @@ def run_ensembles(G, args, rank, barrier):
         ens.init()
         return ens
 
-    tune = tune_ensemble(make, time_blocks=(256, 512, 1024), blocks=2)
-    T, cta, ppt = tune["best"]
-    full = ensemble_systems(G, 1.0, rank)
+    if args.ensemble_shape:
+        T, cta, ppt = (int(x) for x in args.ensemble_shape.split(","))
+        tune = {"table": []}
+    else:
+        tune = tune_ensemble(make, time_blocks=(256, 512, 1024), blocks=2)
+        T, cta, ppt = tune["best"]
+    full = ensemble_systems(G, args.ensemble_fraction, rank)
     ens = make(T, full)
     ens.set_shape(cta, ppt)
     for _ in range(args.warmup):
@@ -513,6 +517,8 @@ def main():
     ap.add_argument("--sample-steps", type=int, default=512)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ensembles", action="store_true")
+    ap.add_argument("--ensemble-fraction", type=float, default=1.0, help="share of each system's particles")
+    ap.add_argument("--ensemble-shape", default="", help="T,cta,ppt: skip the autotuner")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--learned-particles", type=int, default=1_000_000)
     ap.add_argument("--learned-log-blocks", type=int, default=10)
