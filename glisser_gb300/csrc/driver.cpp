@@ -10,6 +10,7 @@
 #include <chrono>
 #include <ctime>
 #include <fstream>
+#include <future>
 #include <iomanip>
 #include <iostream>
 #include <numeric>
@@ -77,6 +78,15 @@ std::vector<size_t> alive_by_id(const Particles& pa, size_t n_alive)
     return order;
 }
 
+// One track snapshot: particle records from the device when the executor can
+// build them there (dense ids), else the host writer.
+void write_snapshot(Executor& ex, std::ostream& out)
+{
+    if (ex.write_track_device(out)) return;
+    const Particles& pa = ex.particles();
+    write_track(out, ex.planets_snapshot(), pa, alive_by_id(pa, ex.n_alive_host()), ex.t, ex.cfg.write_bary_track);
+}
+
 }  // namespace
 
 int run_main(Executor& ex, bool quiet, bool force, std::string& error)
@@ -112,15 +122,14 @@ int run_main(Executor& ex, bool quiet, bool force, std::string& error)
 
     bool crashed = false;
     std::ofstream trackout, histout;
+    std::future<void> pending_dump;
     auto t_start = std::chrono::steady_clock::now();
     try {
         ex.init();
         uint32_t counter = 0, dump_num = 0, track_num = 1;
         if (cfg.track_every != 0) {
             trackout.open(join(cfg.outfolder, "tracks/track.0.out"), std::ios::binary);
-            const Particles& pa = ex.particles();
-            write_track(trackout, ex.planets_snapshot(), pa, alive_by_id(pa, ex.n_alive_host()), ex.t,
-                        cfg.write_bary_track);
+            write_snapshot(ex, trackout);
         }
         if (cfg.swift_hist_every != 0) {
             histout.open(join(cfg.outfolder, "plhist.out"), std::ios::binary);
@@ -154,8 +163,14 @@ int run_main(Executor& ex, bool quiet, bool force, std::string& error)
                 tout << "Dumping to disk. t = " << ex.t << std::endl;
                 std::ofstream c(join(cfg.outfolder, "dumps/config." + std::to_string(dump_num) + ".out"));
                 c << format_config(out);
-                save_state(cfg, ex.planets_snapshot(), ex.particles(),
-                           join(cfg.outfolder, "dumps/state." + std::to_string(dump_num) + ".out"));
+                // the state is downloaded (pinned staging) now; formatting and
+                // the file write run on a writer thread while the next blocks
+                // integrate (one dump in flight at a time)
+                if (pending_dump.valid()) pending_dump.get();
+                pending_dump = std::async(std::launch::async,
+                                          [cfg, pl = ex.planets_snapshot(), pa = ex.particles(),
+                                           path = join(cfg.outfolder, "dumps/state." + std::to_string(dump_num) +
+                                                                          ".out")]() { save_state(cfg, pl, pa, path); });
                 dump_num++;
             }
             if (track) {
@@ -164,16 +179,19 @@ int run_main(Executor& ex, bool quiet, bool force, std::string& error)
                     trackout.open(join(cfg.outfolder, "tracks/track." + std::to_string(track_num++) + ".out"),
                                   std::ios::binary);
                 }
-                const Particles& pa = ex.particles();
-                write_track(trackout, ex.planets_snapshot(), pa, alive_by_id(pa, ex.n_alive_host()), ex.t,
-                            cfg.write_bary_track);
+                write_snapshot(ex, trackout);
             }
             if (hist) write_plhist_record(histout, ex.planets_snapshot(), ex.t);
         }
         ex.finish();
+        if (pending_dump.valid()) pending_dump.get();
     } catch (const std::exception& e) {
         try {
             ex.finish();
+        } catch (...) {
+        }
+        try {
+            if (pending_dump.valid()) pending_dump.get();
         } catch (...) {
         }
         tout << "Exception caught: " << std::endl << e.what() << std::endl;

@@ -18,7 +18,7 @@
 //    (dG3 = G2 ds, dG2 = G1 ds, dG1 = G0 ds), so the accepted solution
 //    carries an O(tol^2) error instead of O(tol) and no second Stumpff
 //    evaluation is needed for it;
-//  * the default starter is a seventh-order reversion of the time series of
+//  * the default starter is a tenth-order reversion of the time series of
 //    Kepler's equation, accurate to ~1e-16 for steps well inside an orbit,
 //    so the residual test normally accepts it on the first evaluation: one
 //    Stumpff evaluation per drift;
@@ -42,7 +42,7 @@ constexpr int KEP_LAGUERRE_MAX = 200;   // bounded fallback passes
 
 enum Starter : int {
     STARTER_CLASSIC = 0,   // the reference's kepu_guess (src/wh.cpp:188-220)
-    STARTER_SERIES = 1,    // seventh-order time-series reversion, else FP32 Kepler pre-solve
+    STARTER_SERIES = 1,    // tenth-order time-series reversion, else FP32 Kepler pre-solve
     STARTER_LEARNED = 2,   // MLP over drift invariants, classic fallback
 };
 
@@ -203,21 +203,27 @@ __device__ __forceinline__ double starter_series3(double dt, double rinv, double
     return tau * fma(tau, fma(tau, c3, c2), 1.0);
 }
 
-// Seventh-order reversion of the time series of Kepler's equation.
-// With T = t/r0, t/r0 = s + c2 s^2 + ... + c6 s^6 where
+// Tenth-order reversion of the time series of Kepler's equation.
+// With T = t/r0, t/r0 = s + c2 s^2 + ... + c9 s^9 where
 //   c2 = u/(2 r0), c3 = k/(6 r0), c4 = -alpha u/(24 r0), c5 = -alpha k/(120 r0),
-//   c6 = alpha^2 u/(720 r0)   (k = mu - alpha r0)
-// follows from the G-function series; its reversion (Abramowitz & Stegun
-// 3.6.25) in the dimensionless X = c2 T, Y = c3 T^2, Z = c4 T^3, W = c5 T^4,
-// V = c6 T^5 is
-//   s/T = 1 - X + (2X^2 - Y) + (-5X^3 + 5XY - Z)
-//           + (14X^4 - 21X^2 Y + 6XZ + 3Y^2 - W)
-//           + (-42X^5 + 84X^3 Y - 28X^2 Z - 28XY^2 + 7XW + 7YZ - V) + O7.
-// For steps well inside an orbit (|X|, sqrt|Y| ~ 1e-3) the neglected
-// eighth-order terms are ~1e-16, so the FP64 residual check usually accepts
-// this s on the first Stumpff evaluation.  Orders 2-4 are summed in FP64;
-// orders 5-7 (below 1e-9 of s) in FP32.
-__device__ __forceinline__ double starter_series6(double dt, double rinv, double alpha, double u, double k)
+//   c6 = alpha^2 u/(720 r0), c7 = alpha^2 k/(5040 r0), c8 = -alpha^3 u/(40320 r0),
+//   c9 = -alpha^3 k/(362880 r0)   (k = mu - alpha r0)
+// follows from the G-function series.  In the dimensionless X = c2 T,
+// Y = c3 T^2 and A = alpha T^2 (so c4 T^3 = -A X/12, c5 T^4 = -A Y/20,
+// c6 T^5 = A^2 X/360, c7 T^6 = A^2 Y/840, c8 T^7 = -A^3 X/20160,
+// c9 T^8 = -A^3 Y/60480) the reversion (Lagrange inversion; A&S 3.6.25 gives
+// it to seventh order) is
+//   s/T = 1 - X + (2X^2 - Y) + X(A/12 - 5X^2 + 5Y)
+//           + (14X^4 - 21X^2 Y + 3Y^2 - A X^2/2 + A Y/20) + o6 + ... + o10,
+// the order-n term o_n homogeneous of degree n-1 in (X, sqrt|Y|, sqrt|A|).
+// For steps well inside an orbit (|X|, sqrt|Y| ~ 1e-3) the neglected terms
+// are far below 1e-16, so the FP64 residual check accepts this s on the
+// first Stumpff evaluation; orders 8-10 keep that true for eccentric orbits
+// near pericentre (tau^2 up to SERIES_TAU2_MAX).  Orders 2-4 are summed in
+// FP64, orders 5-10 (below 1e-9 of s) in FP32.
+constexpr double SERIES_TAU2_MAX = 0.01;
+
+__device__ __forceinline__ double starter_series(double dt, double rinv, double alpha, double u, double k)
 {
     double T = dt * rinv;
     double T2 = T * T;
@@ -234,12 +240,27 @@ __device__ __forceinline__ double starter_series6(double dt, double rinv, double
     float o5 = fmaf(x2, fmaf(14.0f, x2, -21.0f * y), fmaf(6.0f * x, z, fmaf(3.0f * y, y, -w)));
     float o6 = fmaf(x, fmaf(x2, fmaf(-42.0f, x2, 84.0f * y), fmaf(-28.0f * x, z, fmaf(-28.0f * y, y, 7.0f * w))),
                     fmaf(7.0f * y, z, -v));
-    // seventh order (A&S 3.6.25 b7; c7 T^6 = A^2 Y / 840)
     float x3 = x2 * x;
     float o7 = 8.0f * (x * v + y * w) + 4.0f * z * z + 120.0f * x3 * z + 180.0f * x2 * y * y + 132.0f * x3 * x3 -
                (1.0f / 840.0f) * a * a * y - 36.0f * x2 * w - 72.0f * x * y * z - 330.0f * x2 * x2 * y -
                12.0f * y * y * y;
-    return fma(T, low + (double)(o5 + o6 + o7), T);
+    // orders 8-10, Horner in (x^2, y) inside Horner in a
+    const float y2 = y * y, y3 = y2 * y, y4 = y2 * y2;
+    float p0 = fmaf(fmaf(fmaf(-429.0f, x2, 1287.0f * y), x2, -990.0f * y2), x2, 165.0f * y3);
+    float p1 = fmaf(fmaf(165.0f / 4.0f, x2, -99.0f / 2.0f * y), x2, 33.0f / 4.0f * y2);
+    float p2 = fmaf(-7.0f / 16.0f, x2, 41.0f / 560.0f * y);
+    float o8 = x * fmaf(a, fmaf(a, fmaf(a, 1.0f / 20160.0f, p2), p1), p0);
+    float q0 = fmaf(fmaf(fmaf(fmaf(1430.0f, x2, -5005.0f * y), x2, 5005.0f * y2), x2, -1430.0f * y3), x2, 55.0f * y4);
+    float q1 = fmaf(fmaf(fmaf(-1001.0f / 6.0f, x2, 3289.0f / 12.0f * y), x2, -88.0f * y2), x2, 11.0f / 4.0f * y3);
+    float q2 = fmaf(fmaf(209.0f / 72.0f, x2, -407.0f / 336.0f * y), x2, 41.0f / 1680.0f * y2);
+    float q3 = fmaf(-17.0f / 6048.0f, x2, y * (1.0f / 60480.0f));
+    float o9 = fmaf(a, fmaf(a, fmaf(a, q3, q2), q1), q0);
+    float r0c = fmaf(fmaf(fmaf(fmaf(-442.0f, x2, 1768.0f * y), x2, -2184.0f * y2), x2, 910.0f * y3), x2, -91.0f * y4);
+    float r1c = fmaf(fmaf(fmaf(182.0f / 3.0f, x2, -637.0f / 5.0f * y), x2, 637.0f / 10.0f * y2), x2, -91.0f / 15.0f * y3);
+    float r2c = fmaf(fmaf(-91.0f / 60.0f, x2, 39.0f / 35.0f * y), x2, -403.0f / 4200.0f * y2);
+    float r3c = fmaf(4.0f / 945.0f, x2, -23.0f / 75600.0f * y);
+    float o10 = 11.0f * x * fmaf(a, fmaf(a, fmaf(a, r3c, r2c), r1c), r0c);
+    return fma(T, low + (double)(((o5 + o6) + (o7 + o8)) + (o9 + o10)), T);
 }
 
 struct DriftResult {
@@ -332,7 +353,7 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
     } else if (starter == STARTER_CLASSIC) {
         s = starter_classic(dt, r0, rinv, mu, alpha, u);
     } else {
-        if (lt_nonneg(tau2, 0.0025)) s = starter_series6(dt, rinv, alpha, u, k);
+        if (lt_nonneg(tau2, SERIES_TAU2_MAX)) s = starter_series(dt, rinv, alpha, u, k);
         else if (alpha > 0) s = starter_fp32_kepler(dt, r0, mu, alpha, u);
         else s = starter_classic(dt, r0, rinv, mu, alpha, u);
     }

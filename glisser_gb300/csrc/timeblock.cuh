@@ -13,7 +13,12 @@ namespace glisser {
 // chunk is a multiple of 16 bytes for the bulk copy).
 constexpr int LOG_CHUNK = 128;
 constexpr int MAX_PLANETS = 64;           // planets including the Sun
-constexpr int BLOCK_THREADS = 128;
+// Threads per CTA of the single-system kernel (a build-time tuning knob; the
+// CTAs per SM its registers are sized for is GLISSER_TB_MIN_BLOCKS).
+#ifndef GLISSER_TB_THREADS
+#define GLISSER_TB_THREADS 128
+#endif
+constexpr int BLOCK_THREADS = GLISSER_TB_THREADS;
 
 size_t timeblock_smem_bytes(uint32_t npl, int chunk = LOG_CHUNK);
 uint32_t log_chunk_steps(uint32_t npl);

@@ -48,7 +48,7 @@ extern "C" {
 
 /* Kepler starters for the universal-variable drift. */
 #define GLISSER_STARTER_CLASSIC 0  /* the reference's kepu_guess, src/wh.cpp:188-220 */
-#define GLISSER_STARTER_SERIES 1   /* seventh-order time series / FP32 Kepler pre-solve */
+#define GLISSER_STARTER_SERIES 1   /* tenth-order time series / FP32 Kepler pre-solve */
 #define GLISSER_STARTER_LEARNED 2  /* MLP initial guess, classic fallback */
 
 /* Feature normalisation and training box of a learned starter (features
