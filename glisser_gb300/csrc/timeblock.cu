@@ -18,7 +18,7 @@
 // warp ballot and one atomic per warp.
 //
 // Two launches share the tile routine:
-//  * timeblock_kernel: one system, one 128-particle tile per CTA;
+//  * timeblock_kernel: one system, one tile of BLOCK_THREADS particles per CTA;
 //  * batched_kernel: many systems (ensembles), persistent CTAs that pop
 //    (system, tile) items from a device work queue and stage each item's own
 //    planet log; CTA size and particles per thread are template parameters

@@ -16,7 +16,7 @@ constexpr int MAX_PLANETS = 64;           // planets including the Sun
 // Threads per CTA of the single-system kernel (a build-time tuning knob; the
 // CTAs per SM its registers are sized for is GLISSER_TB_MIN_BLOCKS).
 #ifndef GLISSER_TB_THREADS
-#define GLISSER_TB_THREADS 128
+#define GLISSER_TB_THREADS 64
 #endif
 constexpr int BLOCK_THREADS = GLISSER_TB_THREADS;
 

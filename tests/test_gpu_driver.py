@@ -62,9 +62,9 @@ def test_run_writes_reference_layout_and_matches_block_loop(tmp_path):
     assert np.array_equal(got["flags"][o], final["flags"][q])
     assert np.array_equal(got["r"][o], final["r"][q]) and np.array_equal(got["v"][o], final["v"][q])
     # the dump is written in the run's output format (ASCII here) although its
-    # config.N.out asks for binary input -- the reference's behaviour
-    # (targets/main.cpp:208-225 save_data with the run configuration)
-    assert "Read-Binary-Input 1" in open(os.path.join(out, "dumps/config.0.out")).read()
+    # config.N.out says binary output -- the reference's behaviour
+    # (targets/main.cpp:208-225: save_data with the run configuration)
+    assert "Write-Binary-Output 1" in open(os.path.join(out, "dumps/config.0.out")).read()
     d0 = G.Simulation("Input-File %s\nOutput-Folder unused\n" % os.path.join(out, "dumps/state.0.out"))
     d0.load_state()
     dd = d0.particles()
