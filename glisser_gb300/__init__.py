@@ -134,6 +134,8 @@ def lib():
             "glisser_ensemble_set_graph": ([P, C.c_int], C.c_int),
             "glisser_ensemble_set_starter": ([P, C.c_int, C.c_char_p], C.c_int),
             "glisser_ensemble_init": ([P], C.c_int),
+            "glisser_ensemble_set_device_planets": ([P, C.c_int], C.c_int),
+            "glisser_ensemble_get_planets": ([P, C.c_size_t, D, D, D, C.c_size_t, SZ], C.c_int),
             "glisser_ensemble_step": ([P, D], C.c_int),
             "glisser_ensemble_counts": ([P, C.c_size_t, SZ, SZ], C.c_int),
             "glisser_ensemble_get_particles": ([P, C.c_size_t, D, D, U32, U16, C.c_size_t, SZ], C.c_int),
@@ -418,6 +420,18 @@ class Ensemble:
 
     def set_starter(self, starter, mlp_path=None):
         self._check(lib().glisser_ensemble_set_starter(self.h, starter, mlp_path.encode() if mlp_path else None))
+
+    def set_device_planets(self, on=True):
+        """Planet WH on the device (default) or on the host; before init."""
+        self._check(lib().glisser_ensemble_set_device_planets(self.h, int(bool(on))))
+
+    def planets(self, s, cap=64):
+        """Planets of system s at the particles' time (heliocentric)."""
+        m = np.zeros(cap); r = np.zeros((cap, 3)); v = np.zeros((cap, 3))
+        n = C.c_size_t()
+        self._check(lib().glisser_ensemble_get_planets(self.h, s, _p(m, D), _p(r, D), _p(v, D), cap, C.byref(n)))
+        k = n.value
+        return dict(m=m[:k], r=r[:k], v=v[:k])
 
     def init(self):
         self._check(lib().glisser_ensemble_init(self.h))

@@ -556,6 +556,34 @@ int glisser_ensemble_set_starter(glisser_ensemble_t* e, int starter, const char*
         return GLISSER_OK;
     });
 }
+int glisser_ensemble_set_device_planets(glisser_ensemble_t* e, int on)
+{
+    if (!e) return GLISSER_E_INVALID;
+    return guarded_e([&] {
+        e->e->set_device_planets(on != 0);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_ensemble_get_planets(glisser_ensemble_t* e, size_t s, double* m, double* r, double* v, size_t cap,
+                                 size_t* n)
+{
+    if (!e || s >= e->e->systems()) return fail(nullptr, GLISSER_E_INVALID, "glisser_ensemble_get_planets: bad system");
+    return guarded_e([&] {
+        std::vector<double> mm;
+        std::vector<glisser::Vec3> rr, vv;
+        e->e->planets(s, mm, rr, vv);
+        if (n) *n = mm.size();
+        if (cap < mm.size()) throw std::invalid_argument("glisser_ensemble_get_planets: buffer too small");
+        for (size_t k = 0; k < mm.size(); k++) {
+            if (m) m[k] = mm[k];
+            if (r) { r[3 * k] = rr[k].x; r[3 * k + 1] = rr[k].y; r[3 * k + 2] = rr[k].z; }
+            if (v) { v[3 * k] = vv[k].x; v[3 * k + 1] = vv[k].y; v[3 * k + 2] = vv[k].z; }
+        }
+        return GLISSER_OK;
+    });
+}
+
 int glisser_ensemble_init(glisser_ensemble_t* e)
 {
     if (!e) return GLISSER_E_INVALID;

@@ -28,6 +28,7 @@
 #include "ensemble.h"
 #include "executor.h"
 #include "mlp_train.h"
+#include "planets_dev.h"
 #include "timeblock.cuh"
 
 namespace glisser {
@@ -88,11 +89,22 @@ struct Ensemble::Dev {
     uint32_t graph_len[2] = {};
     int graph_starter[2] = { -1, -1 };
     void* d_mlp = nullptr;            // learned-starter weights
+    // device planet integrator state ([S][npl] arrays, one allocation)
+    PlanetSysDev pl{};
+    double* snap[6] = {};             // r, v at the particles' time
+    void* pl_base = nullptr;
+    uint32_t* h_status = nullptr;
+    cudaStream_t pstream = nullptr;
+    cudaEvent_t planets_done = nullptr;
     int mlp_version = 0, graph_mlp[2] = { 0, 0 };
 
     ~Dev()
     {
         mlp_free(d_mlp);
+        cudaFree(pl_base);
+        cudaFreeHost(h_status);
+        if (planets_done) cudaEventDestroy(planets_done);
+        if (pstream) cudaStreamDestroy(pstream);
         for (int b = 0; b < 2; b++) {
             if (graph[b]) cudaGraphExecDestroy(graph[b]);
             cudaFree(d_log[b]); cudaFree(d_m[b]); cudaFree(d_rh[b]); cudaFree(d_id[b]);
@@ -118,6 +130,42 @@ Ensemble::Ensemble(const Config& c, size_t n_systems) : cfg(c), sys_(n_systems),
 }
 
 Ensemble::~Ensemble() = default;
+
+void Ensemble::set_device_planets(bool on)
+{
+    if (initialized_) throw std::invalid_argument("set_device_planets: call before init");
+    device_planets_ = on;
+}
+
+void Ensemble::planets(size_t s, std::vector<double>& m, std::vector<Vec3>& r, std::vector<Vec3>& v)
+{
+    if (s >= sys_.size()) throw std::invalid_argument("system index out of range");
+    const System& y = sys_[s];
+    if (!initialized_ || !device_planets_) {
+        const Planets& src_pl = initialized_ ? y.snap : y.pl;
+        m = src_pl.m;
+        r = src_pl.r;
+        v = src_pl.v;
+        return;
+    }
+    m = y.pl.m;                     // masses do not change
+    r.assign(npl_, Vec3{ 0, 0, 0 });
+    v.assign(npl_, Vec3{ 0, 0, 0 });
+    // the device holds the planets one block ahead of the particles: the
+    // state at the particles' time is the start of the staged block
+    Dev& d = *dev_;
+    ck(cudaStreamSynchronize(d.stream), "sync");
+    ck(cudaStreamSynchronize(d.pstream), "sync");
+    const size_t at = s * npl_;
+    std::vector<double> c(6 * npl_);
+    double* const* src = d.snap;
+    for (int k = 0; k < 6; k++)
+        ck(cudaMemcpy(c.data() + k * npl_, src[k] + at, npl_ * sizeof(double), cudaMemcpyDeviceToHost), "planets");
+    for (uint32_t j = 0; j < npl_; j++) {
+        r[j] = Vec3{ c[j], c[npl_ + j], c[2 * npl_ + j] };
+        v[j] = Vec3{ c[3 * npl_ + j], c[4 * npl_ + j], c[5 * npl_ + j] };
+    }
+}
 
 void Ensemble::set_starter(int s, const std::vector<uint8_t>* mlp_file)
 {
@@ -169,6 +217,7 @@ void Ensemble::planet_block(size_t s, int par)
     Dev& d = *dev_;
     System& y = sys_[s];
     const uint32_t npl = npl_;
+    y.snap = y.pl;
     y.integ.encounter_radii(y.pl, cfg.cull_radius, cfg.encounter_sphere_factor, y.rh);
     double* log = d.h_log[par] + s * log_stride_;
     for (uint32_t k = 0; k < len_; k++) {
@@ -208,6 +257,38 @@ void Ensemble::planets_all(int par)
     for (auto& t : th) t.join();
     for (auto& e : errs)
         if (e) std::rethrow_exception(e);
+}
+
+// The next block's planet logs and encounter radii on the device (one warp
+// per system), on the planet stream; the block's kernel waits for it.
+void Ensemble::planets_device(int par)
+{
+    Dev& d = *dev_;
+    const size_t S = sys_.size(), cnt = S * npl_;
+    const double* src[6] = { d.pl.rx, d.pl.ry, d.pl.rz, d.pl.vx, d.pl.vy, d.pl.vz };
+    for (int k = 0; k < 6; k++)
+        ck(cudaMemcpyAsync(d.snap[k], src[k], cnt * sizeof(double), cudaMemcpyDeviceToDevice, d.pstream), "snapshot");
+    ck(launch_planet_wh(d.pl, (uint32_t)S, npl_, len_, cfg.dt, cfg.cull_radius, cfg.encounter_sphere_factor,
+                        d.d_log[par], log_stride_, d.d_rh[par], d.pstream),
+       "planet kernel");
+    launches_ += 1;
+    ck(cudaMemcpyAsync(d.h_status, d.pl.status, S * sizeof(uint32_t), cudaMemcpyDeviceToHost, d.pstream), "status");
+    ck(cudaEventRecord(d.planets_done, d.pstream), "event");
+}
+
+void Ensemble::check_planet_status()
+{
+    Dev& d = *dev_;
+    ck(cudaEventSynchronize(d.planets_done), "planet kernel");
+    for (size_t s = 0; s < sys_.size(); s++) {
+        uint32_t st = d.h_status[s];
+        if (!st) continue;
+        uint32_t planet = st >> 8;
+        if ((st & 0xFF) == 1) throw StateError("unbound orbit of planet " + std::to_string(planet) + " (system " +
+                                               std::to_string(s) + ")");
+        throw StateError("Unconverging kepler (system " + std::to_string(s) + ", planet " + std::to_string(planet) +
+                         ")");
+    }
 }
 
 void Ensemble::rebuild_tiles(uint32_t tile)
@@ -363,9 +444,59 @@ void Ensemble::init()
     d.h_ho_dti = hmalloc<uint32_t>(cap, "pinned");
     d.h_ho_flags = hmalloc<uint16_t>(cap, "pinned");
     rebuild_tiles(shape_.cta * shape_.ppt);
+    if (device_planets_ && npl_ > PLANET_WH_MAX_NPL) device_planets_ = false;   // host planets beyond 32 bodies
+    if (device_planets_) {
+        // planet state for the device integrator, masses and ids (constant)
+        const size_t cnt = S * npl_;
+        ck(cudaStreamCreateWithFlags(&d.pstream, cudaStreamNonBlocking), "stream");
+        ck(cudaEventCreateWithFlags(&d.planets_done, cudaEventDisableTiming), "event");
+        ck(cudaMalloc(&d.pl_base, cnt * 20 * sizeof(double) + S * sizeof(uint32_t)), "cudaMalloc planets");
+        double* q = static_cast<double*>(d.pl_base);
+        double** arr[14] = { &d.pl.rx, &d.pl.ry, &d.pl.rz, &d.pl.vx, &d.pl.vy, &d.pl.vz, &d.pl.ax, &d.pl.ay,
+                             &d.pl.az, &d.pl.jx, &d.pl.jy, &d.pl.jz, &d.pl.m, &d.pl.eta };
+        for (int k = 0; k < 14; k++) {
+            *arr[k] = q;
+            q += cnt;
+        }
+        for (int k = 0; k < 6; k++) {
+            d.snap[k] = q;
+            q += cnt;
+        }
+        d.pl.status = reinterpret_cast<uint32_t*>(q);
+        d.h_status = hmalloc<uint32_t>(S, "pinned");
+        std::vector<double> h(14 * cnt);
+        for (size_t s = 0; s < S; s++) {
+            System& y = sys_[s];
+            const auto& rj = y.integ.jacobi_r();
+            const auto& acc = y.integ.acc();
+            const auto& eta = y.integ.eta();
+            for (uint32_t j = 0; j < npl_; j++) {
+                const size_t at = s * npl_ + j;
+                const Vec3 a = j ? acc[j] : Vec3{ 0, 0, 0 };
+                const double vals[14] = { y.pl.r[j].x, y.pl.r[j].y, y.pl.r[j].z, y.pl.v[j].x, y.pl.v[j].y,
+                                          y.pl.v[j].z, a.x, a.y, a.z, rj[j].x, rj[j].y, rj[j].z, y.pl.m[j], eta[j] };
+                for (int k = 0; k < 14; k++) h[k * cnt + at] = vals[k];
+                for (int b = 0; b < 2; b++) {
+                    d.h_m[b][at] = y.pl.m[j];
+                    d.h_id[b][at] = y.pl.id[j];
+                }
+            }
+        }
+        ck(cudaMemcpy(d.pl.rx, h.data(), 14 * cnt * sizeof(double), cudaMemcpyHostToDevice), "upload planets");
+        ck(cudaMemset(d.pl.status, 0, S * sizeof(uint32_t)), "memset");
+        for (int b = 0; b < 2; b++) {
+            ck(cudaMemcpy(d.d_m[b], d.h_m[b], cnt * sizeof(double), cudaMemcpyHostToDevice), "upload m");
+            ck(cudaMemcpy(d.d_id[b], d.h_id[b], cnt * sizeof(uint32_t), cudaMemcpyHostToDevice), "upload ids");
+        }
+    }
     initialized_ = true;
     par_ = 0;
-    planets_all(par_);
+    if (device_planets_) {
+        planets_device(par_);
+        check_planet_status();
+    } else {
+        planets_all(par_);
+    }
 }
 
 // Enqueues one block on the stream: uploads, counter reset, kernel, counters back.
@@ -373,11 +504,15 @@ void Ensemble::enqueue(int par)
 {
     Dev& d = *dev_;
     const size_t S = sys_.size();
-    ck(cudaMemcpyAsync(d.d_log[par], d.h_log[par], S * log_stride_ * sizeof(double), cudaMemcpyHostToDevice,
-                       d.stream), "upload log");
-    ck(cudaMemcpyAsync(d.d_m[par], d.h_m[par], S * npl_ * sizeof(double), cudaMemcpyHostToDevice, d.stream), "m");
-    ck(cudaMemcpyAsync(d.d_rh[par], d.h_rh[par], S * npl_ * sizeof(double), cudaMemcpyHostToDevice, d.stream), "rh");
-    ck(cudaMemcpyAsync(d.d_id[par], d.h_id[par], S * npl_ * sizeof(uint32_t), cudaMemcpyHostToDevice, d.stream), "id");
+    if (!device_planets_) {
+        ck(cudaMemcpyAsync(d.d_log[par], d.h_log[par], S * log_stride_ * sizeof(double), cudaMemcpyHostToDevice,
+                           d.stream), "upload log");
+        ck(cudaMemcpyAsync(d.d_m[par], d.h_m[par], S * npl_ * sizeof(double), cudaMemcpyHostToDevice, d.stream), "m");
+        ck(cudaMemcpyAsync(d.d_rh[par], d.h_rh[par], S * npl_ * sizeof(double), cudaMemcpyHostToDevice, d.stream),
+           "rh");
+        ck(cudaMemcpyAsync(d.d_id[par], d.h_id[par], S * npl_ * sizeof(uint32_t), cudaMemcpyHostToDevice, d.stream),
+           "id");
+    }
     size_t max_tiles = n_ / 64 + S + 1;
     ck(cudaMemcpyAsync(d.d_items[par], d.h_items[par], max_tiles * sizeof(BatchItem), cudaMemcpyHostToDevice,
                        d.stream), "items");
@@ -417,6 +552,7 @@ double Ensemble::step(double* gpu_ms)
     for (auto a : alive_) before_alive += a;
     if (nitems > 0) {
         if (shape_.grid == 0) shape_.grid = default_grid();
+        if (device_planets_) ck(cudaStreamWaitEvent(d.stream, d.planets_done, 0), "wait planets");
         ck(cudaEventRecord(d.k0, d.stream), "event");
         if (use_graph_) {
             const BatchShape& gs = d.graph_shape[par];
@@ -448,8 +584,10 @@ double Ensemble::step(double* gpu_ms)
     // the next block's planets while the kernel runs
     t += cfg.dt * len_;
     par_ ^= 1;
-    planets_all(par_);
+    if (device_planets_) planets_device(par_);
+    else planets_all(par_);
     float ms = 0;
+    if (device_planets_) check_planet_status();
     if (nitems > 0) {
         ck(cudaStreamSynchronize(d.stream), "block");
         ck(cudaEventElapsedTime(&ms, d.k0, d.k1), "elapsed");

@@ -29,6 +29,11 @@ public:
     void set_time_block(uint32_t len) { len_ = len; }
     uint32_t time_block() const { return len_; }
     void set_graph(bool on) { use_graph_ = on; }
+    // Planet WH on the device (one warp per system; default) or on the host
+    // thread pool; set before init.
+    void set_device_planets(bool on);
+    // current planet state of system s (heliocentric)
+    void planets(size_t s, std::vector<double>& m, std::vector<Vec3>& r, std::vector<Vec3>& v);
     // GLISSER_STARTER_*; the learned starter takes a weights file image
     void set_starter(int s, const std::vector<uint8_t>* mlp_file);
     void init();
@@ -46,6 +51,7 @@ public:
 private:
     struct System {
         Planets pl;
+        Planets snap;               // planets at the particles' time (host planet mode)
         PlanetIntegrator integ;
         std::vector<double> rh;
         std::vector<Vec3> r, v;     // start state (host)
@@ -60,7 +66,7 @@ private:
     size_t n_ = 0, log_stride_ = 0;
     int par_ = 0;
     int starter_ = GLISSER_STARTER_SERIES;
-    bool initialized_ = false, use_graph_ = true, host_dirty_ = false;
+    bool initialized_ = false, use_graph_ = true, host_dirty_ = false, device_planets_ = true;
     std::vector<uint16_t> flags_;
     std::vector<uint32_t> ids_;
     std::vector<uint32_t> tile_first_, tile_sys_, tile_alive_;
@@ -69,6 +75,8 @@ private:
 
     void planet_block(size_t s, int par);
     void planets_all(int par);
+    void planets_device(int par);
+    void check_planet_status();
     void rebuild_tiles(uint32_t tile);
     uint32_t write_items(int par);
     void enqueue(int par);

@@ -61,6 +61,11 @@ public:
     Vec3 accelerations(const Planets& p);
     // one kick-drift-kick step (src/wh.cpp:1027-1067); returns h0 after it
     Vec3 step(Planets& p, double dt);
+    // state a device integrator continues from: Jacobi positions and
+    // cumulative masses, the last accelerations
+    const std::vector<Vec3>& jacobi_r() const { return rj_; }
+    const std::vector<double>& eta() const { return eta_; }
+    const std::vector<Vec3>& acc() const { return acc_; }
 
 private:
     std::vector<double> eta_, inv_r3_helio_, inv_r3_jacobi_, mu_;

@@ -11,7 +11,10 @@ namespace glisser {
 
 // Steps per planet-log chunk staged in shared memory (even, so that every
 // chunk is a multiple of 16 bytes for the bulk copy).
-constexpr int LOG_CHUNK = 128;
+#ifndef GLISSER_LOG_CHUNK
+#define GLISSER_LOG_CHUNK 128
+#endif
+constexpr int LOG_CHUNK = GLISSER_LOG_CHUNK;
 constexpr int MAX_PLANETS = 64;           // planets including the Sun
 // Threads per CTA of the single-system kernel (a build-time tuning knob; the
 // CTAs per SM its registers are sized for is GLISSER_TB_MIN_BLOCKS).

@@ -267,6 +267,15 @@ int glisser_ensemble_set_system(glisser_ensemble_t *e, size_t s, size_t npl, con
 int glisser_ensemble_set_shape(glisser_ensemble_t *e, int cta, int ppt, uint32_t grid);
 int glisser_ensemble_set_graph(glisser_ensemble_t *e, int use_graph);
 int glisser_ensemble_set_starter(glisser_ensemble_t *e, int starter, const char *mlp_path);
+/* Planet WH on the device, one warp per system, writing the planet logs the
+ * kernel stages (on = 1, the default; planet counts up to 32 including the
+ * Sun), or on a host thread pool with an upload per block (on = 0).  Call
+ * before glisser_ensemble_init. */
+int glisser_ensemble_set_device_planets(glisser_ensemble_t *e, int on);
+/* Planets of system s at the particles' time: m[npl], r/v[npl][3]
+ * (heliocentric); *n receives npl, cap is the room in m / r / v. */
+int glisser_ensemble_get_planets(glisser_ensemble_t *e, size_t s, double *m, double *r, double *v, size_t cap,
+                                 size_t *n);
 int glisser_ensemble_init(glisser_ensemble_t *e);
 int glisser_ensemble_step(glisser_ensemble_t *e, double *gpu_ms);
 int glisser_ensemble_counts(const glisser_ensemble_t *e, size_t s, size_t *n, size_t *n_alive);
