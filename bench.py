@@ -271,21 +271,26 @@ def run_ensembles(G, args, rank, barrier):
     del ens
     learned = run_ensembles_learned(G, args, cfg % T, full, (cta, ppt), barrier)
     # unbatched comparison: each system through the single-system executor
-    # (same T, same starter), on the first 32 systems
-    ps_plain, el_plain = 0, 0.0
-    for m, pr, pv, r, v in full[:32]:
-        sim = G.Simulation(cfg % T)
-        sim.set_planets(m, pr, pv)
-        sim.set_particles(r, v)
-        sim.init()
-        sim.loop()
-        a = sim.stats()["particle_steps"]
-        t1 = time.perf_counter()
-        for _ in range(2):
+    # (same T), on the first 32 systems, with the series starter and with the
+    # reference's classic starter (the plain method)
+    unbatched = {}
+    for name, st in (("series", G.STARTER_SERIES), ("classic", G.STARTER_CLASSIC)):
+        ps_plain, el_plain = 0, 0.0
+        for m, pr, pv, r, v in full[:32]:
+            sim = G.Simulation(cfg % T)
+            sim.set_planets(m, pr, pv)
+            sim.set_particles(r, v)
+            sim.set_starter(st)
+            sim.init()
             sim.loop()
-        el_plain += time.perf_counter() - t1
-        ps_plain += sim.stats()["particle_steps"] - a
-        del sim
+            a = sim.stats()["particle_steps"]
+            t1 = time.perf_counter()
+            for _ in range(2):
+                sim.loop()
+            el_plain += time.perf_counter() - t1
+            ps_plain += sim.stats()["particle_steps"] - a
+            del sim
+        unbatched[name] = ps_plain / el_plain if el_plain else None
     return {
         "workload": "ensembles: 256 systems (Sun + 4 giants, masses x U(0.9,1.1), a x U(0.95,1.05)), lognormal "
                     "particle counts (median 2e4, clipped 1e3..2e5), %d particles, config-1 distributions, dt=180 d"
@@ -297,8 +302,12 @@ def run_ensembles(G, args, rank, barrier):
         "graph": True, "launches_per_block": (s1["launches"] - s0["launches"]) / args.steps,
         "evals_per_particle_step": (s1["kepler_evals"] - s0["kepler_evals"]) / max(ps, 1),
         "learned": learned,
-        "unbatched_value": ps_plain / el_plain if el_plain else None,
-        "unbatched_sample": "first 32 systems one at a time through the single-system executor, 2 blocks each",
+        "unbatched_value": unbatched["series"],
+        "unbatched_classic_value": unbatched["classic"],
+        "unbatched_sample": "first 32 systems one at a time through the single-system executor, 2 blocks each; "
+                            "series starter, and the reference's classic starter (the plain method)",
+        "learned_batched_vs_plain_classic_unbatched": (learned["value"] / unbatched["classic"]
+                                                       if unbatched["classic"] else None),
     }
 
 
