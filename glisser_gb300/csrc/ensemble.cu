@@ -550,9 +550,15 @@ double Ensemble::step(double* gpu_ms)
     uint32_t nitems = write_items(par);
     uint64_t before_alive = 0;
     for (auto a : alive_) before_alive += a;
+    if (device_planets_) {
+        // this block waits for its planet logs; the next block's planets are
+        // launched before this block's kernel so that their few CTAs take SMs
+        // first and run alongside the persistent kernel
+        ck(cudaStreamWaitEvent(d.stream, d.planets_done, 0), "wait planets");
+        planets_device(par ^ 1);
+    }
     if (nitems > 0) {
         if (shape_.grid == 0) shape_.grid = default_grid();
-        if (device_planets_) ck(cudaStreamWaitEvent(d.stream, d.planets_done, 0), "wait planets");
         ck(cudaEventRecord(d.k0, d.stream), "event");
         if (use_graph_) {
             const BatchShape& gs = d.graph_shape[par];
@@ -584,8 +590,7 @@ double Ensemble::step(double* gpu_ms)
     // the next block's planets while the kernel runs
     t += cfg.dt * len_;
     par_ ^= 1;
-    if (device_planets_) planets_device(par_);
-    else planets_all(par_);
+    if (!device_planets_) planets_all(par_);
     float ms = 0;
     if (device_planets_) check_planet_status();
     if (nitems > 0) {

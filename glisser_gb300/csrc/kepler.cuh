@@ -347,9 +347,11 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
     const double k = fma(-alpha, r0, mu);
     const double tau2 = dt2mu * (rinv * rinv) * rinv;     // (dt / dynamical time)^2
     double s;
+    [[maybe_unused]] bool from_mlp = false;
     if constexpr (LEARNED) {
         s = starter_learned(mlp, dt, rinv, tau2, u, mu_r, alpha);
-        if (!(s > 0)) s = starter_classic(dt, r0, rinv, mu, alpha, u);
+        from_mlp = s > 0;
+        if (!from_mlp) s = starter_classic(dt, r0, rinv, mu, alpha, u);
     } else if (starter == STARTER_CLASSIC) {
         s = starter_classic(dt, r0, rinv, mu, alpha, u);
     } else {
@@ -363,7 +365,7 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
     double fpp = 0, ds = 0, inv_fp = 0;
     bool ok = kepler_newton(s, dt, r0, u, mu, alpha, k, tol, g, fpp, inv_fp, ds, res.evals);
     if constexpr (LEARNED) {
-        if (!ok) {
+        if (!ok && from_mlp) {
             s = starter_classic(dt, r0, rinv, mu, alpha, u);
             ok = kepler_newton(s, dt, r0, u, mu, alpha, k, tol, g, fpp, inv_fp, ds, res.evals);
         }

@@ -137,3 +137,34 @@ def test_scattered_disk_matches_oracle_uv(starter):
     live = want["flags"] == 0
     err = np.linalg.norm(got["r"] - want["r"], axis=1) / np.linalg.norm(want["r"], axis=1)
     assert err[live].max() < POS_TOL * 1.024
+
+
+def test_plain_neptune_full_size_against_oracle():
+    """The reference's CPU-runnable configuration at its full size: Sun +
+    Neptune-mass planet at 30 au, 2,000 particles (a 40-50 au, e < 0.1,
+    i < 5 deg), dt = 180 d, 1e4 steps in blocks of 128, cull radius 0.5 au.
+    Flags, survivors and deathtimes equal to the oracle's at every 10th block;
+    positions within 1e-10 relative per 1e3 steps."""
+    from glisser_gb300 import synth
+    m, pr, pv, r, v = synth.cartesian_state(1, 2000, seed=0)
+    cfg = ("Time-Step 180\nTime-Block-Size 128\nFinal-Time 1e30\nCull-Radius 0.5\nOuter-Limit 300\n"
+           "Input-File unused\nOutput-Folder unused\n")
+    sim = G.Simulation(cfg)
+    sim.set_planets(m, pr, pv)
+    sim.set_particles(r, v)
+    sim.init()
+    ex = O.Exec(m, pr, pv, np.arange(len(m)), r, v, np.arange(len(r)), dt=180.0, tbsize=128, outer_r=300.0,
+                cull_r=0.5)
+    blocks = (10000 + 127) // 128
+    for b in range(blocks):
+        sim.loop()
+        ex.loop()
+        if (b + 1) % 10 == 0 or b == blocks - 1:
+            got, want = by_id(sim.particles()), by_id(ex.particles())
+            assert np.array_equal(got["flags"], want["flags"]), b
+            assert np.array_equal(got["deathtime"], want["deathtime"]), b
+            assert sim.counts()["n_alive"] == ex.counts()["n_alive"]
+            live = want["flags"] == 0
+            steps = (b + 1) * 128
+            err = np.linalg.norm(got["r"] - want["r"], axis=1) / np.linalg.norm(want["r"], axis=1)
+            assert err[live].max() < POS_TOL * max(1.0, steps / 1000.0), (b, err[live].max())

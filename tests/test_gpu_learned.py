@@ -209,3 +209,18 @@ def test_bad_weights_file_is_rejected(tmp_path):
     with pytest.raises(G.GlisserError):
         sim.set_starter(G.STARTER_LEARNED, str(p))
     assert os.path.exists(p)
+
+
+def test_outside_the_training_box_the_classic_starter_runs(trained):
+    """Drifts whose features fall outside the network's training box start
+    from the classic starter: identical iteration counts and results."""
+    tr, _, _, _ = trained
+    nm = tr.norm
+    narrow = L.Trainer(16, seed=1)
+    narrow.params = tr.params
+    narrow.norm = dict(nm, x_lo=np.array([50.0, 50.0, 50.0]), x_hi=np.array([51.0, 51.0, 51.0]))
+    m, pr, pv, r, v = synth.cartesian_state(3, 2048, seed=14)
+    a = L.drift_states(r, v, DT, m[0], G.STARTER_LEARNED, narrow)
+    b = L.drift_states(r, v, DT, m[0], G.STARTER_CLASSIC)
+    assert np.array_equal(a[2], b[2])
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
