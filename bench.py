@@ -48,10 +48,10 @@ def config_text(tbsize, dt, outer=300.0):
             "Input-File unused\nOutput-Folder unused\n" % (dt, tbsize, outer))
 
 
-def make_state(G, n, cfg_id, rank):
+def make_state(G, n, workload, rank):
     from glisser_gb300 import synth
-    w = synth.workload(cfg_id, n=0, seed=0)          # planets: seed 0 on every rank
-    el = synth.workload(cfg_id, n=n, seed=1000 + rank)["el"]
+    w = synth.workload(workload, n=0, seed=0)        # planets: seed 0 on every rank
+    el = synth.workload(workload, n=n, seed=1000 + rank)["el"]
     m = w["pl_m"]
     pr, pv = [np.zeros(3)], [np.zeros(3)]
     for k in range(len(m) - 1):
@@ -144,7 +144,7 @@ def run_reference_arm(args, rank, world):
     G.build()
     O.build()
     n_planets = 4
-    w, m, pr, pv, r, v = make_state(G, args.sample_particles, 2, 0)
+    w, m, pr, pv, r, v = make_state(G, args.sample_particles, "plain-giants", 0)
     ex = O.Exec(m, pr, pv, np.arange(len(m)), r, v, np.arange(len(r)), dt=180.0, tbsize=args.sample_steps)
     p = ex.particles()
     blk = ex.planet_block()
@@ -174,7 +174,7 @@ def run_reference_arm(args, rank, world):
 
 
 def ensemble_systems(G, fraction, rank, n_systems=256):
-    """Config 4 systems as (masses, planet r, planet v, particle r, particle v)."""
+    """Ensemble systems as (masses, planet r, planet v, particle r, particle v)."""
     from glisser_gb300 import synth
     out = []
     for m, pel, el in synth.ensemble_workload(n_systems, seed=1000 * rank, fraction=fraction):
@@ -233,7 +233,7 @@ def run_ensembles_learned(G, args, cfg, full, shape, barrier):
 
 
 def run_ensembles(G, args, rank, barrier):
-    """Config 4 (256 systems, lognormal counts, ~6.2e6 particles): autotuned
+    """Ensembles (256 systems, lognormal counts, ~6.2e6 particles): autotuned
     persistent batched launch vs the same systems run one at a time."""
     from glisser_gb300.autotune import tune_ensemble
     cfg = ("Time-Step 180\nTime-Block-Size %d\nFinal-Time 1e30\nCull-Radius 0.5\nOuter-Limit 300\n"
@@ -293,7 +293,7 @@ def run_ensembles(G, args, rank, barrier):
         unbatched[name] = ps_plain / el_plain if el_plain else None
     return {
         "workload": "ensembles: 256 systems (Sun + 4 giants, masses x U(0.9,1.1), a x U(0.95,1.05)), lognormal "
-                    "particle counts (median 2e4, clipped 1e3..2e5), %d particles, config-1 distributions, dt=180 d"
+                    "particle counts (median 2e4, clipped 1e3..2e5), %d particles, plain-neptune particle distributions, dt=180 d"
                     % n_total,
         "value": ps / el, "unit": UNIT, "blocks": args.steps, "time_block": T,
         "shape": {"threads_per_cta": cta, "particles_per_thread": ppt},
@@ -324,7 +324,7 @@ def run_learned(G, args, rank, barrier):
     T = 512
     dt = 180.0
     cfg = config_text(T, dt, outer=1e5)
-    m, pr, pv, r, v = synth.cartesian_state(3, args.learned_particles, seed=2000 + rank)
+    m, pr, pv, r, v = synth.cartesian_state("scattered-disk", args.learned_particles, seed=2000 + rank)
 
     def make(starter, path=None):
         sim = G.Simulation(cfg)
@@ -441,7 +441,7 @@ def run_history(G, args, rank, barrier):
     from glisser_gb300 import synth
     tmp = tempfile.mkdtemp()
     hist = os.path.join(tmp, "plhist.out")
-    m, pr, pv, r, v = synth.cartesian_state(5, args.history_particles, seed=3000 + rank)
+    m, pr, pv, r, v = synth.cartesian_state("history-encounters", args.history_particles, seed=3000 + rank)
     pre = G.Simulation("Time-Step 0.2\nTime-Block-Size 100\nFinal-Time 1e9\nLimit-Particle-Count 0\n"
                        "Input-File unused\nOutput-Folder unused\n")
     pre.set_planets(m, pr, pv)
@@ -584,7 +584,7 @@ def main():
     G.build()
     starter = {"classic": G.STARTER_CLASSIC, "series": G.STARTER_SERIES}[args.starter]
 
-    w, m, pr, pv, r, v = make_state(G, args.particles, 2, rank)
+    w, m, pr, pv, r, v = make_state(G, args.particles, "plain-giants", rank)
     n_planets = len(m) - 1
     dt = 180.0
     sim = G.Simulation(config_text(args.tbsize, dt))

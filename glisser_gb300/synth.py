@@ -1,9 +1,10 @@
-"""Seeded synthetic workloads with the shapes and distributions of the five
-benchmark configurations (orbital elements; angles in radians).
+"""Seeded synthetic workloads (orbital elements; angles in radians): the five
+benchmark workloads, named for what they are -- plain-neptune, plain-giants,
+scattered-disk, ensembles, history-encounters.
 
 The reference ships no particle state for its examples (the 200,000-particle
 resonance state is not distributed), so every workload here is generated:
-numpy's default generator seeded per configuration draws the elements and
+numpy's default generator seeded per workload draws the elements and
 `from_elements_M` (src/convert.cpp:257-275, restated in the library) turns
 them into heliocentric Cartesian states.
 """
@@ -35,7 +36,8 @@ def particle_elements(rng, n, a_range, e_range, i_max_deg, log_a=False):
 
 
 def neptune_planets(gm_sun=GM_SUN_AU_DAY, a=30.0):
-    """Sun + one Neptune-mass planet on a circular, planar orbit (configs 1, 3, 5).
+    """Sun + one Neptune-mass planet on a circular, planar orbit (plain-neptune,
+    scattered-disk, history-encounters).
     Returns (masses [2], elements [1, 6])."""
     m = np.array([gm_sun, NEPTUNE_MASS * gm_sun])
     el = np.array([[a, 0.0, 0.0, 0.0, 0.0, 0.0]])
@@ -43,7 +45,7 @@ def neptune_planets(gm_sun=GM_SUN_AU_DAY, a=30.0):
 
 
 def giant_planets(rng, gm_sun=GM_SUN_AU_DAY, mass_scale=None, a_scale=None):
-    """Sun + four giants with e~U(0,0.05), i~U(0,2 deg) (configs 2, 4)."""
+    """Sun + four giants with e~U(0,0.05), i~U(0,2 deg) (plain-giants, ensembles)."""
     ms = GIANT_MASSES * (mass_scale if mass_scale is not None else 1.0)
     a = GIANT_A * (a_scale if a_scale is not None else 1.0)
     e = rng.uniform(0, 0.05, 4)
@@ -53,23 +55,24 @@ def giant_planets(rng, gm_sun=GM_SUN_AU_DAY, mass_scale=None, a_scale=None):
     return m, np.stack([a, e, inc, O, o, M], axis=1)
 
 
-CONFIGS = {
-    1: dict(name="plain-neptune", n=2000, dt=180.0, steps=10000, tbsize=128, cull=0.5, outer=300.0,
-            planets="neptune", a=(40, 50), e=(0, 0.1), i=5.0),
-    2: dict(name="plain-giants", n=1_000_000, dt=180.0, steps=200_000, tbsize=2048, cull=0.5, outer=300.0,
-            planets="giants", a=(53, 57), e=(0, 0.3), i=10.0),
-    3: dict(name="scattered-disk", n=1_000_000, dt=180.0, steps=50_000, tbsize=512, cull=0.5, outer=1e5,
-            planets="neptune", a=(30, 1000), e=(0, 0.95), i=40.0, log_a=True),
-    4: dict(name="ensembles", systems=256, median=20000, clip=(1000, 200000), dt=180.0, steps=10000, tbsize=1024,
-            cull=0.5, outer=300.0, planets="giants", a=(40, 50), e=(0, 0.1), i=5.0),
-    5: dict(name="history-encounters", n=2_000_000, dt=0.2, steps=50_000, tbsize=100, cull=0.5, outer=300.0,
-            planets="neptune-yr", a=(20, 40), e=(0, 0.3), i=10.0, esf=3.0, hist_every=100),
+WORKLOADS = {
+    "plain-neptune": dict(n=2000, dt=180.0, steps=10000, tbsize=128, cull=0.5, outer=300.0,
+                          planets="neptune", a=(40, 50), e=(0, 0.1), i=5.0),
+    "plain-giants": dict(n=1_000_000, dt=180.0, steps=200_000, tbsize=2048, cull=0.5, outer=300.0,
+                         planets="giants", a=(53, 57), e=(0, 0.3), i=10.0),
+    "scattered-disk": dict(n=1_000_000, dt=180.0, steps=50_000, tbsize=512, cull=0.5, outer=1e5,
+                           planets="neptune", a=(30, 1000), e=(0, 0.95), i=40.0, log_a=True),
+    "ensembles": dict(systems=256, median=20000, clip=(1000, 200000), dt=180.0, steps=10000, tbsize=1024,
+                      cull=0.5, outer=300.0, planets="giants", a=(40, 50), e=(0, 0.1), i=5.0),
+    "history-encounters": dict(n=2_000_000, dt=0.2, steps=50_000, tbsize=100, cull=0.5, outer=300.0,
+                               planets="neptune-yr", a=(20, 40), e=(0, 0.3), i=10.0, esf=3.0, hist_every=100),
 }
 
 
-def workload(cfg_id, n=None, seed=0):
-    """Returns dict(pl_m [npl], pl_el [npl-1, 6], el [n, 6], **cfg) for a config."""
-    c = dict(CONFIGS[cfg_id])
+def workload(name, n=None, seed=0):
+    """Returns dict(pl_m [npl], pl_el [npl-1, 6], el [n, 6], name, **parameters)
+    for the named workload."""
+    c = dict(WORKLOADS[name], name=name)
     rng = np.random.default_rng(seed)
     if c["planets"] == "neptune":
         m, pel = neptune_planets()
@@ -84,7 +87,7 @@ def workload(cfg_id, n=None, seed=0):
 
 
 def ensemble_counts(systems=256, median=20000, clip=(1000, 200000), sigma=0.6, seed=0):
-    """Lognormal particle counts per system (config 4; sigma 0.6 gives ~6e6
+    """Lognormal particle counts per system (ensembles; sigma 0.6 gives ~6e6
     particles over 256 systems)."""
     rng = np.random.default_rng(seed)
     c = np.exp(rng.normal(np.log(median), sigma, systems))
@@ -92,9 +95,9 @@ def ensemble_counts(systems=256, median=20000, clip=(1000, 200000), sigma=0.6, s
 
 
 def ensemble_workload(systems=256, seed=0, fraction=1.0, counts=None):
-    """Config 4: per system (planet masses [5], planet elements [4, 6],
+    """Ensembles: per system (planet masses [5], planet elements [4, 6],
     particle elements [n, 6]); giant masses x U(0.9, 1.1) and semi-major axes
-    x U(0.95, 1.05) per system, particles with the config-1 distributions.
+    x U(0.95, 1.05) per system, particles with the plain-neptune distributions.
     Sub-seed per system = seed + system index.  `fraction` keeps that share of
     every system's particles (at least one)."""
     if counts is None:
@@ -109,13 +112,13 @@ def ensemble_workload(systems=256, seed=0, fraction=1.0, counts=None):
     return out
 
 
-def cartesian_state(cfg_id, n, seed, planet_seed=0):
-    """Planets (m [npl], r [npl, 3], v [npl, 3]; Sun at the origin) from the
-    configuration drawn with `planet_seed`, and n particles (r, v [n, 3])
+def cartesian_state(name, n, seed, planet_seed=0):
+    """Planets (m [npl], r [npl, 3], v [npl, 3]; Sun at the origin) of the
+    named workload drawn with `planet_seed`, and n particles (r, v [n, 3])
     drawn with `seed`, heliocentric."""
     from . import elements_to_cartesian
-    w = workload(cfg_id, n=0, seed=planet_seed)
-    el = workload(cfg_id, n=n, seed=seed)["el"]
+    w = workload(name, n=0, seed=planet_seed)
+    el = workload(name, n=n, seed=seed)["el"]
     m = w["pl_m"]
     pr, pv = [np.zeros(3)], [np.zeros(3)]
     for k in range(len(m) - 1):

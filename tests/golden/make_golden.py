@@ -207,8 +207,8 @@ def main():
     L = ref()
     tmp = tempfile.mkdtemp(prefix="glisser_golden_")
 
-    # --- config 1 shape: Sun + Neptune-mass planet, 200 particles, 8 blocks of 128
-    w = synth.workload(1, n=200, seed=0)
+    # --- plain-neptune shape: Sun + Neptune-mass planet, 200 particles, 8 blocks of 128
+    w = synth.workload("plain-neptune", n=200, seed=0)
     m = w["pl_m"]
     prr, pvv = cartesian(L, m[0] + m[1], w["pl_el"])
     pl_r = np.vstack([np.zeros(3), prr]); pl_v = np.vstack([np.zeros(3), pvv])
@@ -216,8 +216,8 @@ def main():
     run_case(L, tmp, "neptune", ["Time-Step 180", "Time-Block-Size 128", "Final-Time 1e9"],
              m, pl_r, pl_v, r, v, 8, "neptune_t128.npz")
 
-    # --- config 2 shape: Sun + four giants, 128 particles near the 3:1, 4 blocks of 256
-    w = synth.workload(2, n=128, seed=0)
+    # --- plain-giants shape: Sun + four giants, 128 particles near the 3:1, 4 blocks of 256
+    w = synth.workload("plain-giants", n=128, seed=0)
     m = w["pl_m"]
     pl_r = [np.zeros(3)]; pl_v = [np.zeros(3)]
     for k in range(4):
@@ -241,7 +241,7 @@ def main():
 
     # --- Hill-sphere encounters by planet id (Encounter-RH-Factor > 0), 4 giants
     rng = np.random.default_rng(11)
-    w = synth.workload(2, n=4, seed=3)
+    w = synth.workload("plain-giants", n=4, seed=3)
     m = w["pl_m"]
     pl_r = [np.zeros(3)]; pl_v = [np.zeros(3)]
     for k in range(4):
@@ -320,7 +320,7 @@ def main():
     print("wrote elements.npz")
 
     # --- file formats written by the reference writers
-    w = synth.workload(1, n=40, seed=2)
+    w = synth.workload("plain-neptune", n=40, seed=2)
     m = w["pl_m"]
     prr, pvv = cartesian(L, m[0] + m[1], w["pl_el"])
     pl_r = np.vstack([np.zeros(3), prr]); pl_v = np.vstack([np.zeros(3), pvv])

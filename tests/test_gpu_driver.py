@@ -25,7 +25,7 @@ def native():
 
 
 def test_run_writes_reference_layout_and_matches_block_loop(tmp_path):
-    m, pr, pv, r, v = synth.cartesian_state(1, 3000, seed=41)
+    m, pr, pv, r, v = synth.cartesian_state("plain-neptune", 3000, seed=41)
     base = "Time-Step 180\nTime-Block-Size 64\nCull-Radius 0.5\n"
     pre = G.Simulation(base + "Input-File unused\nOutput-Folder unused\n")
     pre.set_planets(m, pr, pv)

@@ -118,7 +118,7 @@ def test_scattered_disk_matches_oracle_uv(starter):
     reference's own elliptic drift stops at 5 Danby passes and flags 0x04 on
     some of these orbits, so its universal-variable spec is the comparison."""
     from glisser_gb300 import synth
-    m, pr, pv, r, v = synth.cartesian_state(3, 512, seed=31)
+    m, pr, pv, r, v = synth.cartesian_state("scattered-disk", 512, seed=31)
     cfg = ("Time-Step 180\nTime-Block-Size 128\nFinal-Time 1e30\nCull-Radius 0.5\nOuter-Limit 1e5\n"
            "Input-File unused\nOutput-Folder unused\n")
     sim = G.Simulation(cfg)
@@ -146,7 +146,7 @@ def test_plain_neptune_full_size_against_oracle():
     Flags, survivors and deathtimes equal to the oracle's at every 10th block;
     positions within 1e-10 relative per 1e3 steps."""
     from glisser_gb300 import synth
-    m, pr, pv, r, v = synth.cartesian_state(1, 2000, seed=0)
+    m, pr, pv, r, v = synth.cartesian_state("plain-neptune", 2000, seed=0)
     cfg = ("Time-Step 180\nTime-Block-Size 128\nFinal-Time 1e30\nCull-Radius 0.5\nOuter-Limit 300\n"
            "Input-File unused\nOutput-Folder unused\n")
     sim = G.Simulation(cfg)

@@ -33,7 +33,7 @@ def native():
 
 
 def simulation(n, seed, T=64, starter=G.STARTER_SERIES, mlp_path=None):
-    m, pr, pv, r, v = synth.cartesian_state(3, n, seed)
+    m, pr, pv, r, v = synth.cartesian_state("scattered-disk", n, seed)
     sim = G.Simulation(CFG % T)
     sim.set_planets(m, pr, pv)
     sim.set_particles(r, v)
@@ -140,7 +140,7 @@ def test_inference_matches_oracle(trained):
 
 def test_learned_starter_saves_newton_passes(trained):
     tr, _, _, _ = trained
-    m, pr, pv, r, v = synth.cartesian_state(3, 8192, seed=12)     # held out
+    m, pr, pv, r, v = synth.cartesian_state("scattered-disk", 8192, seed=12)     # held out
     mu = m[0]
     out = {}
     for name, st in (("classic", G.STARTER_CLASSIC), ("learned", G.STARTER_LEARNED), ("series", G.STARTER_SERIES)):
@@ -177,7 +177,7 @@ def test_ensemble_learned_matches_series_and_is_launch_invariant(trained):
     _, _, _, path = trained
     systems = []
     for s in range(3):
-        m, pr, pv, r, v = synth.cartesian_state(3, [300, 900, 129][s], seed=20 + s)
+        m, pr, pv, r, v = synth.cartesian_state("scattered-disk", [300, 900, 129][s], seed=20 + s)
         systems.append((m, pr, pv, r, v))
 
     def run(starter, cta=128, ppt=1, graph=True):
@@ -219,7 +219,7 @@ def test_outside_the_training_box_the_classic_starter_runs(trained):
     narrow = L.Trainer(16, seed=1)
     narrow.params = tr.params
     narrow.norm = dict(nm, x_lo=np.array([50.0, 50.0, 50.0]), x_hi=np.array([51.0, 51.0, 51.0]))
-    m, pr, pv, r, v = synth.cartesian_state(3, 2048, seed=14)
+    m, pr, pv, r, v = synth.cartesian_state("scattered-disk", 2048, seed=14)
     a = L.drift_states(r, v, DT, m[0], G.STARTER_LEARNED, narrow)
     b = L.drift_states(r, v, DT, m[0], G.STARTER_CLASSIC)
     assert np.array_equal(a[2], b[2])

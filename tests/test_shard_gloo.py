@@ -17,7 +17,7 @@ CFG = "Time-Step 180\nTime-Block-Size 128\nFinal-Time 1e30\nInput-File x\nOutput
 
 def _state():
     from glisser_gb300 import synth
-    m, pr, pv, r, v = synth.cartesian_state(1, 1001, seed=4)
+    m, pr, pv, r, v = synth.cartesian_state("plain-neptune", 1001, seed=4)
     return m, pr, pv, r, v, np.arange(1001, dtype=np.uint32) * 3 + 5     # sparse ids
 
 
