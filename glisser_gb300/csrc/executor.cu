@@ -190,6 +190,19 @@ bool Executor::write_track_device(std::ostream& out, double* ms)
     return true;
 }
 
+void Executor::set_deathtime(uint32_t id, double t)
+{
+    if (dt_dense_on_ && id < dt_dense_.size()) dt_dense_[id] = t;
+    else deathtime_[id] = t;
+}
+
+double Executor::get_deathtime(uint32_t id) const
+{
+    if (dt_dense_on_ && id < dt_dense_.size()) return dt_dense_[id];
+    auto it = deathtime_.find(id);
+    return it == deathtime_.end() ? 0.0 : it->second;
+}
+
 void Executor::device_view(glisser_particles* pa, size_t* n, double* dt, double* mu) const
 {
     if (!initialized_) throw std::invalid_argument("device_view: call init first");
@@ -207,7 +220,7 @@ void Executor::device_view(glisser_particles* pa, size_t* n, double* dt, double*
 void Executor::load()
 {
     load_state(cfg, pl_, pa_);
-    for (size_t k = 0; k < pa_.n; k++) deathtime_[pa_.id[k]] = pa_.deathtime[k];
+    for (size_t k = 0; k < pa_.n; k++) set_deathtime(pa_.id[k], pa_.deathtime[k]);
     loaded_pl_ = loaded_pa_ = true;
     t = cfg.t_0;
 }
@@ -240,7 +253,7 @@ void Executor::set_particles(size_t n, const double* r, const double* v, const u
             pa_.id[k] = id ? id[k] : (uint32_t)k;
             pa_.flags[k] = flags ? flags[k] : 0;
             pa_.deathtime[k] = deathtime ? deathtime[k] : 0.0;
-            deathtime_[pa_.id[k]] = pa_.deathtime[k];
+            set_deathtime(pa_.id[k], pa_.deathtime[k]);
         }
         loaded_pa_ = true;
         return;
@@ -301,17 +314,17 @@ void Executor::initial_accelerations(std::vector<Vec3>& acc)
             double irij3 = 1. / (r2 * std::sqrt(r2));
             a -= dr * (pl_.m[j] * irij3);
             if (r2 < rh_[j] * rh_[j]) {
-                deathtime_[pa_.id[k]] = 0;   // the reference stamps time 0 here
+                set_deathtime(pa_.id[k], 0);   // the reference stamps time 0 here
                 pa_.flags[k] = (uint16_t)((j << 8) | 0x0001);
             }
         }
         double r2 = pa_.r[k].lensq();
         if (r2 < rh_[0] * rh_[0]) {
-            deathtime_[pa_.id[k]] = 0;
+            set_deathtime(pa_.id[k], 0);
             pa_.flags[k] = 0x0001;
         }
         if (r2 > cfg.outer_radius * cfg.outer_radius) {
-            deathtime_[pa_.id[k]] = 0;
+            set_deathtime(pa_.id[k], 0);
             pa_.flags[k] = 0x0002;
         }
         acc[k] = a;
@@ -365,8 +378,7 @@ void Executor::download_particles()
         pa_.id[k] = d.h_dl_u32[k];
         pa_.deathtime_index[k] = d.h_dl_u32[n + k];
         pa_.flags[k] = d.h_dl_flags[k];
-        auto it = deathtime_.find(pa_.id[k]);
-        pa_.deathtime[k] = it == deathtime_.end() ? 0.0 : it->second;
+        pa_.deathtime[k] = get_deathtime(pa_.id[k]);
     }
     host_dirty_ = false;
 }
@@ -578,6 +590,15 @@ void Executor::init()
 
     max_id_ = 0;
     for (size_t k = 0; k < pa_.n; k++) max_id_ = std::max(max_id_, pa_.id[k]);
+    // dense ids: deathtimes in a vector indexed by id (the per-download lookup
+    // is then a load, not a hash probe)
+    if ((size_t)max_id_ <= 4 * pa_.n + 4096) {
+        dt_dense_.assign((size_t)max_id_ + 1, 0.0);
+        for (const auto& e : deathtime_)
+            if (e.first <= max_id_) dt_dense_[e.first] = e.second;
+        deathtime_.clear();
+        dt_dense_on_ = true;
+    }
     d.max_npl = (uint32_t)std::min<size_t>(pl_.n, MAX_PLANETS);
     if (pl_.n > (size_t)MAX_PLANETS) throw StateError("more than 64 planets");
     d.log_cap = (cfg.tbsize + 1u) & ~1u;
@@ -748,7 +769,7 @@ bool Executor::step_block(double* cpu_ms, double* gpu_ms)
                       [](const FlaggedEntry& a, const FlaggedEntry& b) { return a.id < b.id; });
             float tf = (float)t;
             for (auto& f : flagged_) {
-                deathtime_[f.id] = tf;
+                set_deathtime(f.id, tf);
                 if ((f.flags & 0x04) && log)
                     *log << "warning - particle " << f.id << " did not converge on GPU" << std::endl;
                 if (encounter_out) {

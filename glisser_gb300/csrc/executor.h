@@ -86,6 +86,10 @@ private:
     Planets snapshot_;      // planets at the particles' time
     Particles pa_;          // host mirror in device order
     std::unordered_map<uint32_t, double> deathtime_;
+    std::vector<double> dt_dense_;          // deathtimes by id when ids are dense (after init)
+    bool dt_dense_on_ = false;
+    void set_deathtime(uint32_t id, double t);
+    double get_deathtime(uint32_t id) const;
     bool loaded_pl_ = false, loaded_pa_ = false, initialized_ = false, host_dirty_ = false;
 
     PlanetIntegrator integ_;

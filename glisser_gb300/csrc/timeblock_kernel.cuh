@@ -17,8 +17,14 @@ using namespace tile;
 #define GLISSER_TB_MIN_BLOCKS 8
 #endif
 
+// The learned-starter kernel carries the MLP's 32 hidden activations on top
+// of the drift's registers.
+#ifndef GLISSER_TB_MIN_BLOCKS_LEARNED
+#define GLISSER_TB_MIN_BLOCKS_LEARNED GLISSER_TB_MIN_BLOCKS
+#endif
+
 template <int NP, bool LEARNED>
-__global__ void __launch_bounds__(BLOCK_THREADS, GLISSER_TB_MIN_BLOCKS)
+__global__ void __launch_bounds__(BLOCK_THREADS, LEARNED ? GLISSER_TB_MIN_BLOCKS_LEARNED : GLISSER_TB_MIN_BLOCKS)
     timeblock_kernel(const Common p, const double* log, const double* m, const double* rh, const uint32_t* pid,
                      uint32_t n)
 {
