@@ -13,6 +13,7 @@
 #include "config.h"
 #include "executor.h"
 #include "mlp_train.h"
+#include "parallel.h"
 #include "orbits.h"
 #include "state_io.h"
 #include "timeblock.cuh"
@@ -306,14 +307,16 @@ int glisser_get_particles(const glisser_t* h, double* r, double* v, uint32_t* id
         const glisser::Particles& pa = exec_of(hh).particles();
         if (n) *n = pa.n;
         if (cap < pa.n) return fail(hh, GLISSER_E_INVALID, "glisser_get_particles: buffer too small");
-        for (size_t k = 0; k < pa.n; k++) {
-            if (r) { r[3 * k] = pa.r[k].x; r[3 * k + 1] = pa.r[k].y; r[3 * k + 2] = pa.r[k].z; }
-            if (v) { v[3 * k] = pa.v[k].x; v[3 * k + 1] = pa.v[k].y; v[3 * k + 2] = pa.v[k].z; }
-            if (id) id[k] = pa.id[k];
-            if (flags) flags[k] = pa.flags[k];
-            if (deathtime) deathtime[k] = pa.deathtime[k];
-            if (deathtime_index) deathtime_index[k] = pa.deathtime_index[k];
-        }
+        glisser::parallel_for(pa.n, [&](size_t b, size_t e) {
+            for (size_t k = b; k < e; k++) {
+                if (r) { r[3 * k] = pa.r[k].x; r[3 * k + 1] = pa.r[k].y; r[3 * k + 2] = pa.r[k].z; }
+                if (v) { v[3 * k] = pa.v[k].x; v[3 * k + 1] = pa.v[k].y; v[3 * k + 2] = pa.v[k].z; }
+                if (id) id[k] = pa.id[k];
+                if (flags) flags[k] = pa.flags[k];
+                if (deathtime) deathtime[k] = pa.deathtime[k];
+                if (deathtime_index) deathtime_index[k] = pa.deathtime_index[k];
+            }
+        });
         return GLISSER_OK;
     });
 }

@@ -16,6 +16,7 @@
 // reads it (outputs, the C ABI), not every block.
 #include "executor.h"
 #include "interp.h"
+#include "parallel.h"
 #include "track.h"
 
 #include <algorithm>
@@ -266,10 +267,12 @@ void Executor::set_particles(size_t n, const double* r, const double* v, const u
     // ids and the carried accelerations stay on the device
     Impl& d = *d_;
     double* st = d.h_dl;
-    for (size_t k = 0; k < n; k++) {
-        st[k] = r[3 * k]; st[n + k] = r[3 * k + 1]; st[2 * n + k] = r[3 * k + 2];
-        st[3 * n + k] = v[3 * k]; st[4 * n + k] = v[3 * k + 1]; st[5 * n + k] = v[3 * k + 2];
-    }
+    parallel_for(n, [&](size_t b, size_t e) {
+        for (size_t k = b; k < e; k++) {
+            st[k] = r[3 * k]; st[n + k] = r[3 * k + 1]; st[2 * n + k] = r[3 * k + 2];
+            st[3 * n + k] = v[3 * k]; st[4 * n + k] = v[3 * k + 1]; st[5 * n + k] = v[3 * k + 2];
+        }
+    });
     glisser_particles& p = d.buf[d.cur].p;
     glisser_particles& q = d.buf[d.cur ^ 1].p;
     double* dst[6] = { p.rx, p.ry, p.rz, p.vx, p.vy, p.vz };
@@ -372,14 +375,16 @@ void Executor::download_particles()
        "download deathtime index");
     ck(cudaMemcpyAsync(d.h_dl_flags, p.flags, n * sizeof(uint16_t), cudaMemcpyDeviceToHost, d.main), "download flags");
     ck(cudaStreamSynchronize(d.main), "download sync");
-    for (size_t k = 0; k < n; k++) {
-        pa_.r[k] = Vec3{ d.h_dl[k], d.h_dl[n + k], d.h_dl[2 * n + k] };
-        pa_.v[k] = Vec3{ d.h_dl[3 * n + k], d.h_dl[4 * n + k], d.h_dl[5 * n + k] };
-        pa_.id[k] = d.h_dl_u32[k];
-        pa_.deathtime_index[k] = d.h_dl_u32[n + k];
-        pa_.flags[k] = d.h_dl_flags[k];
-        pa_.deathtime[k] = get_deathtime(pa_.id[k]);
-    }
+    parallel_for(n, [&](size_t b, size_t e) {
+        for (size_t k = b; k < e; k++) {
+            pa_.r[k] = Vec3{ d.h_dl[k], d.h_dl[n + k], d.h_dl[2 * n + k] };
+            pa_.v[k] = Vec3{ d.h_dl[3 * n + k], d.h_dl[4 * n + k], d.h_dl[5 * n + k] };
+            pa_.id[k] = d.h_dl_u32[k];
+            pa_.deathtime_index[k] = d.h_dl_u32[n + k];
+            pa_.flags[k] = d.h_dl_flags[k];
+            pa_.deathtime[k] = get_deathtime(pa_.id[k]);
+        }
+    });
     host_dirty_ = false;
 }
 
