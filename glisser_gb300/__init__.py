@@ -127,6 +127,7 @@ def lib():
             "glisser_fp64_peak_probe": ([D, D], C.c_int),
             "glisser_launches": ([P, C.POINTER(C.c_ulonglong)], C.c_int),
             "glisser_l2_flush": ([P, C.c_size_t], C.c_int),
+            "glisser_wait_check": ([C.c_double, U32, D], C.c_int),
             "glisser_stream": ([P, C.POINTER(P)], C.c_int),
             "glisser_ensemble_create": ([C.c_char_p, C.c_size_t, C.POINTER(P)], C.c_int),
             "glisser_ensemble_set_system": ([P, C.c_size_t, C.c_size_t, D, D, D, C.c_size_t, D, D], C.c_int),
@@ -225,6 +226,17 @@ def l2_flush(stream, nbytes=256 << 20):
     rc = lib().glisser_l2_flush(C.c_void_p(stream), nbytes)
     if rc:
         _raise(rc, last_error())
+
+
+def wait_check(limit_seconds=0.05):
+    """Bounded-wait self-test: (status, elapsed seconds); status carries
+    the staging-timeout bit when the wait gave up as it should."""
+    st = C.c_uint32()
+    el = C.c_double()
+    rc = lib().glisser_wait_check(limit_seconds, C.byref(st), C.byref(el))
+    if rc:
+        _raise(rc, last_error())
+    return st.value, el.value
 
 
 def to_elements(mu, r, v):

@@ -19,6 +19,7 @@
 #include "timeblock.cuh"
 
 namespace glisser {
+int wait_check(double limit_seconds, uint32_t* status_out, double* elapsed_out);
 size_t partition_scratch_bytes(size_t n);
 int launch_partition(const glisser_particles* in, const glisser_particles* out, size_t n, void* scratch,
                      uint32_t* n0, uint32_t* n1, cudaStream_t stream);
@@ -848,3 +849,10 @@ int glisser_kepler_drift_states(const glisser_particles* pa, size_t n, double dt
 }
 
 }  // extern "C"
+
+extern "C" int glisser_wait_check(double limit_seconds, uint32_t* status, double* elapsed)
+{
+    int rc = glisser::wait_check(limit_seconds, status, elapsed);
+    if (rc != GLISSER_OK) return fail(nullptr, rc, "glisser_wait_check: bad limit or CUDA failure");
+    return GLISSER_OK;
+}

@@ -58,13 +58,28 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
 
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-// Bounded wait: ~2^22 polls (each poll may itself suspend briefly).
-constexpr uint32_t WAIT_POLLS = 1u << 22;
+// Bounded wait on an mbarrier phase: gives up after WAIT_NS of the global
+// nanosecond timer (or WAIT_POLLS polls, whichever comes first) and returns
+// false, so that a copy that never lands ends the kernel with a status bit
+// instead of a hang.  A staged chunk normally lands in microseconds.
+constexpr uint32_t WAIT_POLLS = 1u << 26;
+constexpr uint64_t WAIT_NS = 2000000000ull;   // 2 s
 
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity)
+__device__ __forceinline__ uint64_t global_ns()
 {
-    for (uint32_t k = 0; k < WAIT_POLLS; k++)
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t limit_ns = WAIT_NS)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    for (uint32_t k = 0; k < WAIT_POLLS; k++) {
         if (mbar_try_wait(bar, parity)) return true;
+        if ((k & 63u) == 0 && global_ns() - t0 > limit_ns) return false;
+    }
     return false;
 }
 

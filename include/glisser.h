@@ -303,6 +303,13 @@ int glisser_fp64_peak_probe(double *tflops, double *ms);
  * no reference counterpart. */
 int glisser_l2_flush(void *stream, size_t bytes);
 
+/* Self-test of the bounded wait that guards the planet-log staging: arms a
+ * shared-memory barrier that nothing will complete and waits with the kernels'
+ * own routine and a limit of limit_seconds (0 < limit <= 10).  *status
+ * receives GLISSER_STATUS_LOG_TIMEOUT when the wait gave up (the expected
+ * outcome), *elapsed the seconds it waited; the context stays usable. */
+int glisser_wait_check(double limit_seconds, uint32_t *status, double *elapsed);
+
 /* ------------------------------------------------------------------------
  * Learned Kepler starter.  No counterpart in the reference (its drift,
  * src/wh.cu:43-110, always starts Newton from the same analytic guess).  A
