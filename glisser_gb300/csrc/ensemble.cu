@@ -2,16 +2,22 @@
 // planets and particles, integrated block by block in one persistent launch.
 //
 // Per block:
-//   host  : every system's planet WH for the block (a thread pool over
-//           systems) into pinned staging; the (system, tile) work items of
-//           the tiles that still hold alive particles;
+//   device, planet stream: the next block's planet WH for every system (one
+//           warp per system, planets_dev.cu) writing the planet logs and
+//           encounter radii the next block stages, launched just before this
+//           block's kernel so its few CTAs take SMs first;
+//   host  : the (system, tile) work items of the tiles that still hold alive
+//           particles;
 //   device: one CUDA graph per staging parity, captured once: upload of the
-//           planet blocks and the items, reset of the queue and counters, the
-//           persistent batched kernel, counters back to the host;
+//           items, reset of the queue and counters, the persistent batched
+//           kernel, counters back to the host (the graph waits for this
+//           block's planet logs);
 //   host  : the hand-off list updates the per-tile alive counts.
 // Dead particles stay in place (skipped inside their tile); tiles with no
 // alive particle leave the queue, so no per-system partition is needed.
-// The planet work of block k+1 overlaps the kernel of block k.
+// With the host planet path (more than 32 bodies, or switched off) a thread
+// pool integrates every system's planets for the next block into pinned
+// staging while the kernel runs, and the graph uploads them.
 #include <algorithm>
 #include <atomic>
 #include <chrono>

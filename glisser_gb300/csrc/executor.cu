@@ -7,13 +7,16 @@
 //                 epilogue, flagged particles ballot-compacted into the
 //                 hand-off list) -> stable 3-way partition into the second
 //                 particle buffer -> counts and hand-off list to pinned host
-//   host        : snapshot the planets, advance t, integrate or interpolate
-//                 the planets for the next block and upload that log on the
-//                 copy stream into the other planet buffer (overlapped with the
-//                 kernel), then read the counts, stamp deathtimes and write
+//   host        : snapshot the planets, advance t, integrate the planets for
+//                 the next block and upload that log on the copy stream into
+//                 the other planet buffer -- or, with a planetary history,
+//                 upload the interval's element tracks and evaluate every
+//                 step's record on the device (interp.cu) -- overlapped with
+//                 the kernel; then read the counts, stamp deathtimes and write
 //                 encounter.out for the newly flagged particles.
 // The full particle state comes back to the host mirror only when someone
-// reads it (outputs, the C ABI), not every block.
+// reads it (outputs, the C ABI), not every block; track snapshots are built
+// on the device (track.cu).
 #include "executor.h"
 #include "interp.h"
 #include "parallel.h"

@@ -51,8 +51,7 @@ struct __align__(16) MlpDev {
     float b2[MLP_H];
     float w3[MLP_H];
     float b3;
-    uint32_t valid;
-    float pad[2];
+    float pad[3];
     MlpNorm norm;
 };
 

@@ -353,7 +353,6 @@ MlpDev make_dev(const float* params, const MlpNorm& norm)
         d.w3[j] = bf16_round_host(params[MLP_OFF_W3 + j]);
     }
     d.b3 = params[MLP_OFF_B3];
-    d.valid = 1;
     d.norm = norm;
     return d;
 }
