@@ -512,6 +512,29 @@ def run_history(G, args, rank, barrier):
     }
 
 
+def check_accuracy(G, m, pr, pv, r, v, dt, n=4096, steps=1024):
+    """The metric's accuracy bound on this workload: a sample of the particles
+    integrated over `steps` steps by the library and by the oracle's
+    restatement of the reference kernel (src/wh.cu:43-177); max relative
+    position difference of the survivors and whether the flags agree."""
+    from oracle import oracle as O
+    O.build()
+    sim = G.Simulation(config_text(steps, dt))
+    sim.set_planets(m, pr, pv)
+    sim.set_particles(r[:n], v[:n])
+    sim.init()
+    sim.loop()
+    ex = O.Exec(m, pr, pv, np.arange(len(m)), r[:n], v[:n], np.arange(n), dt=dt, tbsize=steps)
+    ex.loop()
+    got, want = sim.particles(), ex.particles()
+    go, wo = np.argsort(got["id"]), np.argsort(want["id"])
+    live = want["flags"][wo] == 0
+    d = np.linalg.norm(got["r"][go] - want["r"][wo], axis=1) / np.linalg.norm(want["r"][wo], axis=1)
+    return {"particles": n, "steps": steps, "max_rel_pos_err_vs_oracle": float(d[live].max()),
+            "flags_identical": bool(np.array_equal(got["flags"][go], want["flags"][wo])),
+            "oracle": "restatement of the reference kernel MVSKernel::step_forward (src/wh.cu:43-177)"}
+
+
 def run_track(G, sim):
     """Track snapshot of the current state (alive particles by id, FP64
     elements, float32 records): device writer vs the host writer, wall time
@@ -691,6 +714,9 @@ def main():
     track = None
     if rank == 0 and not args.no_track:
         track = run_track(G, sim)
+    accuracy = None
+    if rank == 0 and not args.no_cpu_baseline:
+        accuracy = check_accuracy(G, m, pr, pv, r, v, dt)
     del sim
     ensembles = None
     if not args.no_ensembles:
@@ -730,6 +756,7 @@ def main():
             "learned": learned,
             "history": history,
             "track": track,
+            "accuracy": accuracy,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:
