@@ -34,6 +34,7 @@ sys.path.insert(0, ROOT)
 METRIC = "particle-steps/s on 1 GB300, learned+batched vs plain, at <=1e-10 rel pos err"
 UNIT = "particle-steps/s"
 DRAM_BYTES_PER_PARTICLE_BLOCK = 76.6
+KEPLER_TOL_SCATTERED = 1e-14     # the scattered-disk workload's Newton tolerance
 
 
 def alg_flops_per_particle_step(n_planets, k_ref=5):
@@ -331,6 +332,7 @@ def run_learned(G, args, rank, barrier):
         sim.set_planets(m, pr, pv)
         sim.set_particles(r, v)
         sim.set_starter(starter, path)
+        sim.set_kepler_tolerance(KEPLER_TOL_SCATTERED)
         sim.init()
         return sim
 
@@ -401,6 +403,7 @@ def run_learned(G, args, rank, barrier):
         sim.set_planets(m, pr, pv)
         sim.set_particles(r[:ns], v[:ns])
         sim.set_starter(st, path if st == G.STARTER_LEARNED else None)
+        sim.set_kepler_tolerance(KEPLER_TOL_SCATTERED)
         sim.init()
         for _ in range(2):
             sim.loop()
@@ -413,8 +416,8 @@ def run_learned(G, args, rank, barrier):
         del sim
     return {
         "workload": "scattered-disk: Sun + Neptune-mass planet at 30 au, %d particles a~logU(30,1000) au, "
-                    "e~U(0,0.95), i~U(0,40deg), dt=180 d, Time-Block-Size %d, Outer-Limit 1e5 au"
-                    % (args.learned_particles, T),
+                    "e~U(0,0.95), i~U(0,40deg), dt=180 d, Time-Block-Size %d, Outer-Limit 1e5 au, Kepler "
+                    "tolerance %g" % (args.learned_particles, T, KEPLER_TOL_SCATTERED),
         "blocks": args.learned_blocks, "steps_per_leg": (1 + args.learned_blocks) * T,
         "training": {"samples": n_samples, "plain_evals_per_solve": plain_evals / max(n_samples, 1),
                      "log_blocks": args.learned_log_blocks, "log_s": t_log, "steps": args.learned_train_steps,

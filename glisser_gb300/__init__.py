@@ -55,7 +55,7 @@ class PlanetBlockDev(C.Structure):
 
 class StepParams(C.Structure):
     _fields_ = [("dt", C.c_double), ("outer_radius", C.c_double), ("starter", C.c_int32),
-                ("kill_encounters", C.c_int32), ("mlp", C.c_void_p)]
+                ("kill_encounters", C.c_int32), ("mlp", C.c_void_p), ("kepler_tol", C.c_double)]
 
 
 class MlpNorm(C.Structure):
@@ -103,6 +103,8 @@ def lib():
             "glisser_init": ([P], C.c_int),
             "glisser_set_device_interp": ([P, C.c_int], C.c_int),
             "glisser_set_device_output": ([P, C.c_int], C.c_int),
+            "glisser_set_kepler_tolerance": ([P, C.c_double], C.c_int),
+            "glisser_ensemble_set_kepler_tolerance": ([P, C.c_double], C.c_int),
             "glisser_step_block": ([P, C.POINTER(C.c_int), D, D], C.c_int),
             "glisser_run": ([P, C.c_int], C.c_int),
             "glisser_finish": ([P], C.c_int),
@@ -303,6 +305,10 @@ class Simulation:
         """Planetary history per step on the device (default) or the host; before init."""
         self._check(lib().glisser_set_device_interp(self.h, int(bool(on))))
 
+    def set_kepler_tolerance(self, tol):
+        """Kepler residual tolerance |f| < tol * dt (default 1e-13)."""
+        self._check(lib().glisser_set_kepler_tolerance(self.h, tol))
+
     def set_device_output(self, on=True):
         """Track snapshots built on the device (default) or by the host writer."""
         self._check(lib().glisser_set_device_output(self.h, int(bool(on))))
@@ -432,6 +438,10 @@ class Ensemble:
 
     def set_starter(self, starter, mlp_path=None):
         self._check(lib().glisser_ensemble_set_starter(self.h, starter, mlp_path.encode() if mlp_path else None))
+
+    def set_kepler_tolerance(self, tol):
+        """Kepler residual tolerance |f| < tol * dt (default 1e-13)."""
+        self._check(lib().glisser_ensemble_set_kepler_tolerance(self.h, tol))
 
     def set_device_planets(self, on=True):
         """Planet WH on the device (default) or on the host; before init."""

@@ -233,6 +233,15 @@ int glisser_set_device_interp(glisser_t* h, int on)
     });
 }
 
+int glisser_set_kepler_tolerance(glisser_t* h, double tol)
+{
+    if (!(tol >= 1e-16 && tol <= 1e-8)) return fail(h, GLISSER_E_INVALID, "glisser_set_kepler_tolerance: 1e-16 <= tol <= 1e-8");
+    return guarded(h, [&] {
+        exec_of(h).set_kepler_tolerance(tol);
+        return GLISSER_OK;
+    });
+}
+
 int glisser_set_device_output(glisser_t* h, int on)
 {
     return guarded(h, [&] {
@@ -567,6 +576,14 @@ int glisser_ensemble_set_device_planets(glisser_ensemble_t* e, int on)
         e->e->set_device_planets(on != 0);
         return GLISSER_OK;
     });
+}
+
+int glisser_ensemble_set_kepler_tolerance(glisser_ensemble_t* e, double tol)
+{
+    if (!e || !(tol >= 1e-16 && tol <= 1e-8))
+        return fail(nullptr, GLISSER_E_INVALID, "glisser_ensemble_set_kepler_tolerance: 1e-16 <= tol <= 1e-8");
+    e->e->set_kepler_tolerance(tol);
+    return GLISSER_OK;
 }
 
 int glisser_ensemble_get_planets(glisser_ensemble_t* e, size_t s, double* m, double* r, double* v, size_t cap,

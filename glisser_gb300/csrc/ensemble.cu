@@ -94,6 +94,7 @@ struct Ensemble::Dev {
     BatchShape graph_shape[2] = {};
     uint32_t graph_len[2] = {};
     int graph_starter[2] = { -1, -1 };
+    double graph_tol[2] = { -1, -1 };
     void* d_mlp = nullptr;            // learned-starter weights
     // device planet integrator state ([S][npl] arrays, one allocation)
     PlanetSysDev pl{};
@@ -532,6 +533,7 @@ void Ensemble::enqueue(int par)
     sp.starter = starter_;
     sp.kill_encounters = 1;
     sp.mlp = starter_ == GLISSER_STARTER_LEARNED ? d.d_mlp : nullptr;
+    sp.kepler_tol = kepler_tol_;
     glisser_handoff ho{};
     ho.count = d.d_ctr;
     ho.status = d.d_ctr + 1;
@@ -570,7 +572,7 @@ double Ensemble::step(double* gpu_ms)
             const BatchShape& gs = d.graph_shape[par];
             bool stale = !d.graph[par] || gs.cta != shape_.cta || gs.ppt != shape_.ppt || gs.grid != shape_.grid ||
                          d.graph_len[par] != len_ || d.graph_starter[par] != starter_ ||
-                         d.graph_mlp[par] != d.mlp_version;
+                         d.graph_mlp[par] != d.mlp_version || d.graph_tol[par] != kepler_tol_;
             if (stale) {
                 if (d.graph[par]) cudaGraphExecDestroy(d.graph[par]);
                 d.graph[par] = nullptr;
@@ -584,6 +586,7 @@ double Ensemble::step(double* gpu_ms)
                 d.graph_shape[par] = shape_;
                 d.graph_starter[par] = starter_;
                 d.graph_mlp[par] = d.mlp_version;
+                d.graph_tol[par] = kepler_tol_;
             }
             ck(cudaGraphLaunch(d.graph[par], d.stream), "graph launch");
             launches_ += 1;

@@ -32,6 +32,8 @@ public:
     // Planet WH on the device (one warp per system; default) or on the host
     // thread pool; set before init.
     void set_device_planets(bool on);
+    // Kepler residual tolerance |f| < tol * dt of the drift (0: 1e-13).
+    void set_kepler_tolerance(double tol) { kepler_tol_ = tol; }
     // current planet state of system s (heliocentric)
     void planets(size_t s, std::vector<double>& m, std::vector<Vec3>& r, std::vector<Vec3>& v);
     // GLISSER_STARTER_*; the learned starter takes a weights file image
@@ -66,6 +68,7 @@ private:
     size_t n_ = 0, log_stride_ = 0;
     int par_ = 0;
     int starter_ = GLISSER_STARTER_SERIES;
+    double kepler_tol_ = 0;
     bool initialized_ = false, use_graph_ = true, host_dirty_ = false, device_planets_ = true;
     std::vector<uint16_t> flags_;
     std::vector<uint32_t> ids_;

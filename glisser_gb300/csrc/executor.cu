@@ -712,6 +712,7 @@ bool Executor::step_block(double* cpu_ms, double* gpu_ms)
         sp.starter = starter_;
         sp.kill_encounters = cfg.resolve_encounters ? 0 : 1;
         sp.mlp = starter_ == GLISSER_STARTER_LEARNED ? d.d_mlp : nullptr;
+        sp.kepler_tol = kepler_tol_;
         glisser_handoff ho{};
         ho.count = d.d_ctr;
         ho.status = d.d_ctr + 1;

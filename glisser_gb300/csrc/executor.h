@@ -64,6 +64,8 @@ public:
     // Planetary history evaluated per step on the device (default) or on the
     // host (the reference's arrangement); set before init.
     void set_device_interp(bool on) { device_interp_ = on; }
+    // Kepler residual tolerance |f| < tol * dt of the drift (0: 1e-13).
+    void set_kepler_tolerance(double tol) { kepler_tol_ = tol; }
     // Track snapshots built on the device (default) or by the host writer.
     void set_device_output(bool on) { device_output_ = on; }
     // Writes a track snapshot with the particle records built on the device
@@ -100,6 +102,7 @@ private:
     bool starting_interval_ = false;
     int starter_ = GLISSER_STARTER_SERIES;
     bool device_interp_ = true;
+    double kepler_tol_ = 0;
     bool device_output_ = true;
     uint32_t max_id_ = 0;
     unsigned long long evals_total_ = 0;

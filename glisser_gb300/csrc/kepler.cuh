@@ -324,7 +324,8 @@ __device__ __forceinline__ bool kepler_laguerre(double& s, double dt, double r0,
 }
 
 // Drifts (r, v) by dt about a central mass mu.  dt2mu = dt^2 mu (a per-
-// block constant: the step-size test compares tau^2 = dt^2 mu / r0^3).
+// block constant: the step-size test compares tau^2 = dt^2 mu / r0^3);
+// tol_dt = the residual tolerance times dt (KEP_TOL * dt by default).
 // LEARNED selects the MLP starter (weights `mlp`), with the classic starter
 // outside the network's training box and as the restart when the Newton
 // passes from the learned guess do not converge; otherwise `starter` picks
@@ -332,7 +333,7 @@ __device__ __forceinline__ bool kepler_laguerre(double& s, double dt, double r0,
 template <bool LEARNED>
 __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, double& rz, double& vx, double& vy, double& vz,
                                                    double r2, double dt, double mu, double dt2mu, int starter,
-                                                   const MlpDev* mlp)
+                                                   const MlpDev* mlp, double tol_dt)
 {
     double v2 = fma(vx, vx, fma(vy, vy, vz * vz));
     double u = fma(rx, vx, fma(ry, vy, rz * vz));
@@ -360,7 +361,7 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
         else s = starter_classic(dt, r0, rinv, mu, alpha, u);
     }
 
-    const double tol = KEP_TOL * dt;
+    const double tol = tol_dt;
     GFun g;
     double fpp = 0, ds = 0, inv_fp = 0;
     bool ok = kepler_newton(s, dt, r0, u, mu, alpha, k, tol, g, fpp, inv_fp, ds, res.evals);

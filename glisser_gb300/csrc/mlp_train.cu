@@ -311,7 +311,7 @@ __global__ void drift_states_kernel(glisser_particles pa, uint32_t n, double dt,
     if (i >= n) return;
     double rx = pa.rx[i], ry = pa.ry[i], rz = pa.rz[i], vx = pa.vx[i], vy = pa.vy[i], vz = pa.vz[i];
     const double r2 = fma(rx, rx, fma(ry, ry, rz * rz));
-    DriftResult d = kepler_drift<LEARNED>(rx, ry, rz, vx, vy, vz, r2, dt, mu, dt * dt * mu, starter, mlp);
+    DriftResult d = kepler_drift<LEARNED>(rx, ry, rz, vx, vy, vz, r2, dt, mu, dt * dt * mu, starter, mlp, KEP_TOL * dt);
     pa.rx[i] = rx; pa.ry[i] = ry; pa.rz[i] = rz;
     pa.vx[i] = vx; pa.vy[i] = vy; pa.vz[i] = vz;
     if (evals) evals[i] = d.evals;

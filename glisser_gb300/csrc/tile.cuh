@@ -15,6 +15,7 @@ struct Common {
     uint32_t chunk;
     double dt;
     double outer2;
+    double tol_dt;          // Kepler residual tolerance x dt
     int starter;
     int kill;
     const MlpDev* mlp;
@@ -207,7 +208,7 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
             for (int k = 0; k < PPT; k++) {
                 if (flags[k] != 0) continue;
                 DriftResult d = kepler_drift<LEARNED>(rx[k], ry[k], rz[k], vx[k], vy[k], vz[k], r2[k], p.dt, mu, dt2mu,
-                                                       p.starter, p.mlp);
+                                                       p.starter, p.mlp, p.tol_dt);
                 uint16_t fl = d.flags;
                 evals += d.evals;
                 double aax = L[0], aay = L[1], aaz = L[2];
@@ -317,6 +318,7 @@ inline bool fill_common(Common& p, const glisser_particles* pa, const glisser_st
     p.len = len;
     p.dt = sp->dt;
     p.outer2 = sp->outer_radius * sp->outer_radius;
+    p.tol_dt = (sp->kepler_tol > 0 ? sp->kepler_tol : KEP_TOL) * sp->dt;
     p.starter = sp->starter;
     p.kill = sp->kill_encounters;
     p.mlp = reinterpret_cast<const MlpDev*>(sp->mlp);

@@ -58,6 +58,7 @@ int launch_timeblock(const glisser_particles* pa, size_t n_alive, const glisser_
     if (n_alive > 0xFFFFFFF0ull) return GLISSER_E_INVALID;
     if (!handoff_ok(ho)) return GLISSER_E_INVALID;
     if (!(sp->dt > 0) || !(sp->outer_radius >= 0)) return GLISSER_E_INVALID;
+    if (!(sp->kepler_tol == 0 || (sp->kepler_tol >= 1e-16 && sp->kepler_tol <= 1e-8))) return GLISSER_E_INVALID;
     if (pl->len > 0) {
         if (!pl->log || !pl->m || !pl->id || !pl->rh) return GLISSER_E_INVALID;
         if (((uintptr_t)pl->log & 15u) != 0) return GLISSER_E_INVALID;

@@ -99,6 +99,7 @@ typedef struct glisser_step_params {
     int32_t starter;             /* GLISSER_STARTER_* */
     int32_t kill_encounters;     /* nonzero: 0x01 -> 0x80 at block end (KillEncounterKernel) */
     const void *mlp;             /* learned-starter weights (device), or NULL */
+    double kepler_tol;           /* Kepler residual tolerance |f| < tol*dt; 0 = 1e-13 (the reference's DANBYB) */
 } glisser_step_params;
 
 /* Hand-off of the particles flagged during a block, compacted by warp ballot
@@ -189,6 +190,12 @@ int glisser_set_particles(glisser_t *h, size_t n, const double *r, const double 
  * reference's arrangement, src/interp.cpp:113-165).  Call before init. */
 int glisser_set_device_interp(glisser_t *h, int on);
 
+/* Kepler residual tolerance of the drift's Newton iteration, |f| < tol * dt
+ * (the reference's DANBYB is 1e-13, the default); 1e-16 <= tol <= 1e-8.  The
+ * accepted Newton correction is folded into the G-functions, so the solution
+ * error is O(tol^2). */
+int glisser_set_kepler_tolerance(glisser_t *h, double tol);
+
 /* Track snapshots (glisser_write_track) with the particle records built on
  * the device -- elements, float32 packing and id order in kernels, one
  * device-to-host copy -- (on = 1, the default) or by the host writer (on =
@@ -272,6 +279,7 @@ int glisser_ensemble_set_starter(glisser_ensemble_t *e, int starter, const char 
  * Sun), or on a host thread pool with an upload per block (on = 0).  Call
  * before glisser_ensemble_init. */
 int glisser_ensemble_set_device_planets(glisser_ensemble_t *e, int on);
+int glisser_ensemble_set_kepler_tolerance(glisser_ensemble_t *e, double tol);
 /* Planets of system s at the particles' time: m[npl], r/v[npl][3]
  * (heliocentric); *n receives npl, cap is the room in m / r / v. */
 int glisser_ensemble_get_planets(glisser_ensemble_t *e, size_t s, double *m, double *r, double *v, size_t cap,

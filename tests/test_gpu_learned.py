@@ -224,3 +224,32 @@ def test_outside_the_training_box_the_classic_starter_runs(trained):
     b = L.drift_states(r, v, DT, m[0], G.STARTER_CLASSIC)
     assert np.array_equal(a[2], b[2])
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_tighter_kepler_tolerance(trained):
+    """The scattered-disk workload's Newton tolerance, |f| < 1e-14 dt: the
+    same flags, positions within 1e-10 of the default-tolerance run, at most
+    a few more Stumpff evaluations per step; out-of-range tolerances are
+    refused."""
+    _, _, _, path = trained
+    runs = {}
+    for tol in (None, 1e-14):
+        sim, _ = simulation(2048, seed=16, T=128)
+        if tol:
+            sim.set_kepler_tolerance(tol)
+        for _ in range(4):
+            sim.loop()
+        p = sim.particles()
+        o = np.argsort(p["id"])
+        runs[tol] = (p["r"][o], p["flags"][o], sim.stats())
+    a, b = runs[None], runs[1e-14]
+    assert np.array_equal(a[1], b[1])
+    live = a[1] == 0
+    err = np.linalg.norm(a[0] - b[0], axis=1) / np.linalg.norm(a[0], axis=1)
+    assert err[live].max() < 1e-10
+    ev_a = a[2]["kepler_evals"] / a[2]["particle_steps"]
+    ev_b = b[2]["kepler_evals"] / b[2]["particle_steps"]
+    assert ev_a <= ev_b < ev_a + 0.2
+    sim, _ = simulation(16, seed=17, T=16)
+    with pytest.raises(G.GlisserError):
+        sim.set_kepler_tolerance(1e-20)
