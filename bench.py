@@ -560,10 +560,30 @@ def run_track(G, sim):
     finally:
         if os.path.exists(path):
             os.remove(path)
+    # dump stream: the full state back from the device (pinned staging) and
+    # the binary state file (the driver's dumps use the same calls)
+    dpath = os.path.join(d, "glisser_dump_%d.out" % os.getpid())
+    try:
+        sim.set_particles(*(lambda p: (p["r"], p["v"]))(sim.particles()))    # mark the host mirror stale
+        t0 = time.perf_counter()
+        st = sim.particles()
+        dl_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        sim.write_state(dpath, binary=True)
+        wr_s = time.perf_counter() - t0
+        dsize = os.path.getsize(dpath)
+    finally:
+        if os.path.exists(dpath):
+            os.remove(dpath)
+    state_bytes = len(st["r"]) * (6 * 8 + 4 + 4 + 2)
     n = sim.counts()["n_alive"]
     return {"particles": n, "bytes": size, "device_ms": dev_s * 1e3, "host_ms": host_s * 1e3,
             "device_GBps": size / dev_s / 1e9, "host_GBps": size / host_s / 1e9,
-            "note": "wall time of glisser_write_track (kernels + device-to-host copy + file write to %s)" % d}
+            "note": "wall time of glisser_write_track (kernels + device-to-host copy + file write to %s)" % d,
+            "dump": {"download_bytes": state_bytes, "download_ms": dl_s * 1e3,
+                     "download_GBps": state_bytes / dl_s / 1e9, "file_bytes": dsize, "write_ms": wr_s * 1e3,
+                     "note": "glisser_get_particles after an upload (device-to-host through pinned staging and the "
+                             "host mirror), then glisser_write_state binary"}}
 
 
 def main():

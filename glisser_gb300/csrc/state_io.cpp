@@ -9,9 +9,11 @@
 //    misreads its own binary dumps);
 //  * readers check for truncation and throw instead of leaving zeros.
 #include "state_io.h"
+#include "parallel.h"
 
 #include <cctype>
 #include <cmath>
+#include <cstring>
 #include <fstream>
 #include <iomanip>
 #include <limits>
@@ -189,13 +191,21 @@ void save_state_binary(std::ostream& out, const Config& cfg, const Planets& pl, 
         put(out, pl.v[i].x * m); put(out, pl.v[i].y * m); put(out, pl.v[i].z * m);
     }
     put<uint64_t>(out, pa.n);
-    for (size_t i = 0; i < pa.n; i++) {
-        put<uint32_t>(out, pa.id[i]);
-        put(out, pa.r[i].x); put(out, pa.r[i].y); put(out, pa.r[i].z);
-        put(out, pa.v[i].x); put(out, pa.v[i].y); put(out, pa.v[i].z);
-        put<uint16_t>(out, pa.flags[i]);
-        put<double>(out, pa.deathtime[i]);
-    }
+    // packed 62-byte records (id, r, v, flags, deathtime) formatted in memory
+    // across the host cores, then one write
+    constexpr size_t REC = 4 + 6 * 8 + 2 + 8;
+    std::vector<char> buf(pa.n * REC);
+    parallel_for(pa.n, [&](size_t b, size_t e) {
+        for (size_t i = b; i < e; i++) {
+            char* q = buf.data() + i * REC;
+            const double rv[6] = { pa.r[i].x, pa.r[i].y, pa.r[i].z, pa.v[i].x, pa.v[i].y, pa.v[i].z };
+            std::memcpy(q, &pa.id[i], 4);
+            std::memcpy(q + 4, rv, 48);
+            std::memcpy(q + 52, &pa.flags[i], 2);
+            std::memcpy(q + 54, &pa.deathtime[i], 8);
+        }
+    });
+    out.write(buf.data(), (std::streamsize)buf.size());
 }
 
 void save_state(const Config& cfg, const Planets& pl, const Particles& pa, const std::string& path)
