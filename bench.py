@@ -352,6 +352,21 @@ def run_learned(G, args, rank, barrier):
     t_train = time.perf_counter() - t0
     path = os.path.join(tempfile.mkdtemp(), "starter.bin")
     tr.save(path)
+    # the guess's relative error in s on held-out drifts (another seed)
+    hm, hpr, hpv, hr, hv = synth.cartesian_state("scattered-disk", 100_000, seed=9000 + rank)
+    hsim = G.Simulation(cfg)
+    hsim.set_planets(hm, hpr, hpv)
+    hsim.set_particles(hr, hv)
+    hsim.init()
+    held = L.Trainer(100_001, seed=1)
+    held.log_simulation(hsim)
+    hf, hz = held.get_samples()
+    zp = tr.predict(hf)
+    ok = np.isfinite(zp) & np.isfinite(hz)
+    rel = np.abs(np.expm1((zp[ok].astype(np.float64) - hz[ok]) * np.exp(hf[ok, 0].astype(np.float64))))
+    guess_err = {"samples": int(ok.sum()), "median": float(np.median(rel)), "q99": float(np.quantile(rel, 0.99)),
+                 "max": float(rel.max()), "outside_box": int((~np.isfinite(zp)).sum())}
+    del hsim, held
 
     legs = {}
     finals = {}
@@ -422,6 +437,7 @@ def run_learned(G, args, rank, barrier):
         "training": {"samples": n_samples, "plain_evals_per_solve": plain_evals / max(n_samples, 1),
                      "log_blocks": args.learned_log_blocks, "log_s": t_log, "steps": args.learned_train_steps,
                      "batch": 16384, "train_s": t_train, "loss_first": float(losses[:10].mean()),
+                     "guess_rel_err_held_out": guess_err,
                      "loss_last": float(losses[-100:].mean()), "network": "3-32-32-1 SiLU, BF16 weights, FP32 accumulate"},
         "starters": legs,
         "learned_vs_classic": legs["learned"]["value"] / legs["classic"]["value"],
