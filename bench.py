@@ -531,6 +531,21 @@ def run_history(G, args, rank, barrier):
     }
 
 
+def hbm_view(traffic_bytes, kernel_ms):
+    """The same launch against the measured HBM copy bandwidth
+    (MEASURED_PEAKS.json): the DRAM side of the time-block kernel."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        peak = json.load(open(path))["hbm_gbs"]
+    except (OSError, ValueError, KeyError):
+        peak = 6800.0
+        src = "fallback 6.8 TB/s"
+    else:
+        src = "measured (MEASURED_PEAKS.json hbm_gbs)"
+    achieved = traffic_bytes / (kernel_ms * 1e-3) / 1e9
+    return {"achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": src}
+
+
 def check_accuracy(G, m, pr, pv, r, v, dt, n=4096, steps=1024):
     """The metric's accuracy bound on this workload: a sample of the particles
     integrated over `steps` steps by the library and by the oracle's
@@ -781,6 +796,7 @@ def main():
                        "l2": "flushed between timed blocks (256 MB write)"},
             "roofline": {"bound": "fp64", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
                          "frac": achieved_tf / peak_tf if peak_tf else None, "traffic": traffic,
+                         "hbm_view": hbm_view(traffic, sum(kernel_ms) / len(kernel_ms)),
                          "kernel": "timeblock_kernel", "flops_per_particle_step": F,
                          "peak_source": "measured FP64 DFMA probe (glisser_fp64_peak_probe); MEASURED_PEAKS.json "
                                         "has no FP64 figure"},
