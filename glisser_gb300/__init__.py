@@ -18,6 +18,8 @@ LIB_PATH = os.path.join(os.environ.get("GLISSER_BUILD_DIR") or os.path.join(HERE
 OK = 0
 E_INVALID, E_CONFIG, E_IO, E_CUDA, E_STATE, E_NOMEM, E_EOS, E_RUNTIME, E_TIMEOUT = range(-1, -10, -1)
 STARTER_CLASSIC, STARTER_SERIES, STARTER_LEARNED = 0, 1, 2
+# StepParams.kill_encounters: what a particle ending the block in an encounter keeps
+ENCOUNTERS_KEEP, ENCOUNTERS_KILL, ENCOUNTERS_ROLLBACK = 0, 1, 2
 FLAG_ENCOUNTER, FLAG_OUT_OF_BOUNDS, FLAG_KEPLER, FLAG_UNBOUND, FLAG_DEAD = 0x01, 0x02, 0x04, 0x08, 0x80
 
 
@@ -166,6 +168,17 @@ def lib():
             "glisser_mlp_device_weights": ([P, C.POINTER(P)], C.c_int),
             "glisser_kepler_drift_states": ([C.POINTER(ParticlesDev), C.c_size_t, C.c_double, C.c_double, C.c_int,
                                              P, P, P, P], C.c_int),
+            "glisser_write_stat": ([P, C.c_char_p], C.c_int),
+            "glisser_swift_write_param": ([C.c_char_p, C.c_double, C.c_size_t, C.c_size_t, C.c_double, C.c_double],
+                                          C.c_int),
+            "glisser_swift_write_tp": ([C.c_char_p, C.c_size_t, D, D, C.c_uint32], C.c_int),
+            "glisser_swift_write_history": ([C.c_char_p, C.c_double, C.c_double, C.c_size_t, U32, D, D, D, D, D],
+                                            C.c_int),
+            "glisser_swift_stats_create": ([C.c_uint32, C.POINTER(P)], C.c_int),
+            "glisser_swift_stats_destroy": ([P], C.c_int),
+            "glisser_swift_read_tpout": ([P, C.c_char_p, C.c_size_t, U32, U32, C.c_size_t, D, D, U16], C.c_int),
+            "glisser_swift_stats_get": ([P, C.c_uint32, C.POINTER(C.c_int32), D], C.c_int),
+            "glisser_swift_write_stat": ([P, C.c_char_p], C.c_int),
             "glisser_partition_noalloc_max_particles": ([], C.c_size_t),
             "glisser_partition_noalloc": ([C.POINTER(ParticlesDev), C.POINTER(ParticlesDev), C.c_size_t, P, P, P],
                                           C.c_int),
@@ -399,6 +412,70 @@ class Simulation:
 
     def write_plhist(self, path, begin=False):
         self._check(lib().glisser_write_plhist(self.h, path.encode(), int(begin)))
+
+    def write_stat(self, path):
+        """stat.out: SWIFT's status of every particle handed to it."""
+        self._check(lib().glisser_write_stat(self.h, path.encode()))
+
+
+def _check_global(rc):
+    if rc:
+        _raise(rc, last_error())
+
+
+def swift_write_param(path, rel_t, prev_len, cur_len, dt, outer_radius):
+    """SWIFT's parameter file for the span [rel_t - prev_len dt, rel_t + cur_len dt]."""
+    _check_global(lib().glisser_swift_write_param(path.encode(), rel_t, prev_len, cur_len, dt, outer_radius))
+
+
+def swift_write_tp(path, r, v, statlen=13):
+    """SWIFT's test-particle file for positions r and velocities v ([n, 3])."""
+    r = np.ascontiguousarray(r, np.float64).reshape(-1, 3)
+    v = np.ascontiguousarray(v, np.float64).reshape(-1, 3)
+    _check_global(lib().glisser_swift_write_tp(path.encode(), len(r), _p(r, D), _p(v, D), statlen))
+
+
+def swift_write_history(path, m0, span, ids, mass, aei_i, oom_i, aei_f, oom_f):
+    """One lookup interval as SWIFT's two-record planetary history."""
+    ids = np.ascontiguousarray(ids, np.uint32)
+    arr = [np.ascontiguousarray(a, np.float64) for a in (mass, aei_i, oom_i, aei_f, oom_f)]
+    _check_global(lib().glisser_swift_write_history(path.encode(), m0, span, len(ids), _p(ids, U32),
+                                                    *[_p(a, D) for a in arr]))
+
+
+class SwiftStats:
+    """SWIFT's per-particle status arrays, accumulated over output files."""
+
+    def __init__(self, statlen=13):
+        h = C.c_void_p()
+        _check_global(lib().glisser_swift_stats_create(statlen, C.byref(h)))
+        self.h = h
+        self.statlen = statlen
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h and _lib is not None:
+            _lib.glisser_swift_stats_destroy(h)
+            self.h = None
+
+    def read_tpout(self, path, ids, planet_ids):
+        """Reads one output file; returns (r, v, flags) of its particles."""
+        ids = np.ascontiguousarray(ids, np.uint32)
+        pids = np.ascontiguousarray(planet_ids, np.uint32)
+        n = len(ids)
+        r = np.zeros((n, 3)); v = np.zeros((n, 3)); fl = np.zeros(n, np.uint16)
+        _check_global(lib().glisser_swift_read_tpout(self.h, path.encode(), n, _p(ids, U32), _p(pids, U32), len(pids),
+                                                     _p(r, D), _p(v, D), _p(fl, U16)))
+        return r, v, fl
+
+    def get(self, pid):
+        """(istat, rstat) of particle pid, or None."""
+        ist = np.zeros(self.statlen, np.int32); rst = np.zeros(self.statlen)
+        rc = lib().glisser_swift_stats_get(self.h, pid, ist.ctypes.data_as(C.POINTER(C.c_int32)), _p(rst, D))
+        return None if rc else (ist, rst)
+
+    def write(self, path):
+        _check_global(lib().glisser_swift_write_stat(self.h, path.encode()))
 
 
 class Ensemble:

@@ -25,6 +25,8 @@ int launch_batched(const glisser_particles* pa, const BatchSystems& sys, const B
     if (!pa || !sp || !ho || !items || !n_items || !queue) return GLISSER_E_INVALID;
     if (npl < 1 || npl > (uint32_t)MAX_PLANETS || !handoff_ok(ho)) return GLISSER_E_INVALID;
     if (!(sp->kepler_tol == 0 || (sp->kepler_tol >= 1e-16 && sp->kepler_tol <= 1e-8))) return GLISSER_E_INVALID;
+    if (sp->kill_encounters < GLISSER_ENCOUNTERS_KEEP || sp->kill_encounters > GLISSER_ENCOUNTERS_ROLLBACK)
+        return GLISSER_E_INVALID;
     if (((uintptr_t)sys.log & 15u) != 0 || (sys.log_stride * sizeof(double)) % 16 != 0) return GLISSER_E_INVALID;
     Common p;
     if (!fill_common(p, pa, sp, ho, npl, len)) return GLISSER_E_INVALID;

@@ -28,6 +28,10 @@ int launch_partition_noalloc(const glisser_particles* in, const glisser_particle
                              uint32_t* n1, cudaStream_t stream);
 }  // namespace glisser
 
+struct glisser_swift_stats {
+    glisser::SwiftStats stats;
+};
+
 struct glisser_s {
     std::unique_ptr<glisser::Executor> ex;
     std::string err;
@@ -415,6 +419,107 @@ int glisser_write_track(const glisser_t* h, const char* path, int append)
         std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return pa.id[a] < pa.id[b]; });
         const glisser::Planets& pl = ex.initialized() ? ex.planets_snapshot() : ex.planets_live();
         glisser::write_track(out, pl, pa, order, ex.t, ex.cfg.write_bary_track);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_write_stat(const glisser_t* h, const char* path)
+{
+    glisser_t* hh = const_cast<glisser_t*>(h);
+    return guarded(hh, [&]() {
+        if (!path) throw std::invalid_argument("glisser_write_stat: null path");
+        std::ofstream out(path);
+        if (!out) throw glisser::IoError(std::string("cannot write ") + path);
+        const glisser::SwiftStats* st = exec_of(hh).swift_stats();
+        if (st) st->write(out);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_swift_write_param(const char* path, double rel_t, size_t prev_len, size_t cur_len, double dt,
+                              double outer_radius)
+{
+    return guarded(nullptr, [&]() {
+        if (!path) throw std::invalid_argument("glisser_swift_write_param: null path");
+        glisser::swift_write_param(path, rel_t, prev_len, cur_len, dt, outer_radius);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_swift_write_tp(const char* path, size_t n, const double* r, const double* v, uint32_t statlen)
+{
+    return guarded(nullptr, [&]() {
+        if (!path || (n && (!r || !v))) throw std::invalid_argument("glisser_swift_write_tp: null argument");
+        glisser::swift_write_tp(path, n, reinterpret_cast<const glisser::Vec3*>(r),
+                                reinterpret_cast<const glisser::Vec3*>(v), statlen);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_swift_write_history(const char* path, double m0, double span, size_t npl, const uint32_t* ids,
+                                const double* mass, const double* aei_i, const double* oom_i, const double* aei_f,
+                                const double* oom_f)
+{
+    return guarded(nullptr, [&]() {
+        if (!path || (npl && (!ids || !mass || !aei_i || !oom_i || !aei_f || !oom_f)))
+            throw std::invalid_argument("glisser_swift_write_history: null argument");
+        glisser::SwiftHistory hst;
+        hst.m0 = m0;
+        hst.span = span;
+        hst.npl = npl;
+        hst.ids = ids;
+        hst.mass = mass;
+        hst.aei_i = reinterpret_cast<const glisser::Vec3*>(aei_i);
+        hst.oom_i = reinterpret_cast<const glisser::Vec3*>(oom_i);
+        hst.aei_f = reinterpret_cast<const glisser::Vec3*>(aei_f);
+        hst.oom_f = reinterpret_cast<const glisser::Vec3*>(oom_f);
+        glisser::swift_write_history(path, hst);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_swift_stats_create(uint32_t statlen, glisser_swift_stats** out)
+{
+    return guarded(nullptr, [&]() {
+        if (!out || statlen < 2) throw std::invalid_argument("glisser_swift_stats_create: bad argument");
+        *out = new glisser_swift_stats{ glisser::SwiftStats(statlen) };
+        return GLISSER_OK;
+    });
+}
+
+int glisser_swift_stats_destroy(glisser_swift_stats* s)
+{
+    delete s;
+    return GLISSER_OK;
+}
+
+int glisser_swift_read_tpout(glisser_swift_stats* s, const char* path, size_t n, const uint32_t* ids,
+                             const uint32_t* planet_ids, size_t n_planet_ids, double* r, double* v, uint16_t* flags)
+{
+    return guarded(nullptr, [&]() {
+        if (!s || !path || (n && (!ids || !r || !v || !flags)) || (n_planet_ids && !planet_ids))
+            throw std::invalid_argument("glisser_swift_read_tpout: null argument");
+        s->stats.read_tpout(path, n, ids, planet_ids, n_planet_ids, reinterpret_cast<glisser::Vec3*>(r),
+                            reinterpret_cast<glisser::Vec3*>(v), flags);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_swift_stats_get(const glisser_swift_stats* s, uint32_t id, int32_t* istat, double* rstat)
+{
+    if (!s) return fail(nullptr, GLISSER_E_INVALID, "glisser_swift_stats_get: null handle");
+    if (!s->stats.get(id, istat, rstat))
+        return fail(nullptr, GLISSER_E_INVALID, "glisser_swift_stats_get: no status for particle " + std::to_string(id));
+    return GLISSER_OK;
+}
+
+int glisser_swift_write_stat(const glisser_swift_stats* s, const char* path)
+{
+    return guarded(nullptr, [&]() {
+        if (!s || !path) throw std::invalid_argument("glisser_swift_write_stat: null argument");
+        std::ofstream out(path);
+        if (!out) throw glisser::IoError(std::string("cannot write ") + path);
+        s->stats.write(out);
         return GLISSER_OK;
     });
 }

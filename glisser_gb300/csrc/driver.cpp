@@ -117,8 +117,10 @@ int run_main(Executor& ex, bool quiet, bool force, std::string& error)
     std::ofstream enc(join(cfg.outfolder, "encounter.out"));
     std::ofstream timelog(join(cfg.outfolder, "time.out"));
     timelog << "start " << now_text() << std::endl;
+    std::ofstream timing(join(cfg.outfolder, "timing.out"));
     ex.log = &tout;
     ex.encounter_out = &enc;
+    ex.timing_out = &timing;
 
     bool crashed = false;
     std::ofstream trackout, histout;
@@ -212,6 +214,7 @@ int run_main(Executor& ex, bool quiet, bool force, std::string& error)
     timelog << "end " << now_text() << std::endl;
     ex.log = nullptr;
     ex.encounter_out = nullptr;
+    ex.timing_out = nullptr;
     return crashed ? -1 : 0;
 }
 

@@ -82,7 +82,7 @@ struct DevParticles {
 }  // namespace
 
 struct Executor::Impl {
-    cudaStream_t main = nullptr, htd = nullptr;
+    cudaStream_t main = nullptr, htd = nullptr, dth = nullptr;
     cudaEvent_t start = nullptr, stop = nullptr, done = nullptr;
     cudaEvent_t uploaded[2] = { nullptr, nullptr };
     DevParticles buf[2];
@@ -150,6 +150,7 @@ struct Executor::Impl {
         if (done) cudaEventDestroy(done);
         if (main) cudaStreamDestroy(main);
         if (htd) cudaStreamDestroy(htd);
+        if (dth) cudaStreamDestroy(dth);
     }
 };
 
@@ -594,7 +595,12 @@ void Executor::init()
         pa_ = std::move(q);
         acc.swap(a2);
     }
-    (void)n_unflagged;
+    initial_flagged_.clear();
+    if (cfg.resolve_encounters)
+        for (size_t k = n_unflagged; k < n_alive; k++) initial_flagged_.push_back({ pa_.id[k], pa_.flags[k], 0 });
+    if (cfg.resolve_encounters)
+        swift_.reset(new SwiftRunner(cfg.swift_path, cfg.outfolder.empty() ? std::string(".") : cfg.outfolder,
+                                     cfg.swift_statlen, cfg.swift_part_min, cfg.num_swift, cfg.outer_radius));
 
     max_id_ = 0;
     for (size_t k = 0; k < pa_.n; k++) max_id_ = std::max(max_id_, pa_.id[k]);
@@ -628,11 +634,13 @@ void Executor::init()
         snapshot_ = pl_;
         initialized_ = true;
         update_planets();
+        if (timing_out) write_timing_header();
         return;
     }
     // device resources
     ck(cudaStreamCreateWithFlags(&d.main, cudaStreamNonBlocking), "stream");
     ck(cudaStreamCreateWithFlags(&d.htd, cudaStreamNonBlocking), "stream");
+    ck(cudaStreamCreateWithFlags(&d.dth, cudaStreamNonBlocking), "stream");
     ck(cudaEventCreate(&d.start), "event");
     ck(cudaEventCreate(&d.stop), "event");
     ck(cudaEventCreateWithFlags(&d.done, cudaEventDisableTiming), "event");
@@ -676,6 +684,7 @@ void Executor::init()
     snapshot_ = pl_;
     initialized_ = true;
     update_planets();
+    if (timing_out) write_timing_header();
     if (log) {
         *log << std::setprecision(7);
         *log << "e_0 (planets) = " << e0 << std::endl;
@@ -691,13 +700,38 @@ bool Executor::step_block(double* cpu_ms, double* gpu_ms)
 {
     if (!initialized_) throw std::runtime_error("step before init");
     Impl& d = *d_;
+    const auto t_total = clk::now();
+    BlockTiming tm;
     const int used = d.blk;
-    const size_t prev_alive = n_dev_;
+    const bool resolve = cfg.resolve_encounters && d.device;
+    // the kernel integrates the unflagged particles; with Resolve-Encounters
+    // the encounter particles that follow them are resumed on SWIFT over the
+    // same block and rejoin at the partition after it
+    const size_t n_kernel = n_dev_;
+    const size_t n_enc = resolve ? n_encounter_ : 0;
+    const size_t n_range = n_kernel + n_enc;
+    const size_t n_enc_start = n_encounter_;
     float gpu = 0;
-    if (n_dev_ > 0) {
-        ck(cudaStreamWaitEvent(d.main, d.uploaded[used], 0), "wait upload");
+    bool partitioned = false;
+    auto launch_partition_now = [&]() {
+        int nxt = d.cur ^ 1;
+        int rc = launch_partition(&d.buf[d.cur].p, &d.buf[nxt].p, n_range, d.d_scratch, d.d_ctr + 2, d.d_ctr + 3,
+                                  d.main);
+        launches_total_ += 3;   // count, scan, scatter
+        if (rc != GLISSER_OK) throw CudaError("partition launch failed");
+        ck(cudaMemcpyAsync(d.h_ctr, d.d_ctr, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, d.main), "counters");
+        ck(cudaMemcpyAsync(d.h_evals, d.d_evals, sizeof(unsigned long long), cudaMemcpyDeviceToHost, d.main), "evals");
+        ck(cudaEventRecord(d.done, d.main), "event");
+        d.cur = nxt;
+        host_dirty_ = true;
+        partitioned = true;
+    };
+    if (n_range > 0) {
         ck(cudaMemsetAsync(d.d_ctr, 0, 16 * sizeof(uint32_t), d.main), "memset counters");
         ck(cudaMemsetAsync(d.d_evals, 0, sizeof(unsigned long long), d.main), "memset evals");
+    }
+    if (n_kernel > 0) {
+        ck(cudaStreamWaitEvent(d.main, d.uploaded[used], 0), "wait upload");
         glisser_planet_block pb{};
         pb.log = d.d_log[used];
         pb.m = d.d_m[used];
@@ -710,7 +744,7 @@ bool Executor::step_block(double* cpu_ms, double* gpu_ms)
         sp.dt = cur_dt_;
         sp.outer_radius = cfg.outer_radius;
         sp.starter = starter_;
-        sp.kill_encounters = cfg.resolve_encounters ? 0 : 1;
+        sp.kill_encounters = cfg.resolve_encounters ? GLISSER_ENCOUNTERS_ROLLBACK : GLISSER_ENCOUNTERS_KILL;
         sp.mlp = starter_ == GLISSER_STARTER_LEARNED ? d.d_mlp : nullptr;
         sp.kepler_tol = kepler_tol_;
         glisser_handoff ho{};
@@ -723,78 +757,341 @@ bool Executor::step_block(double* cpu_ms, double* gpu_ms)
         ho.capacity = (uint32_t)std::max<size_t>(pa_.n, 1);
         ho.evals = d.d_evals;
         ck(cudaEventRecord(d.start, d.main), "event");
-        int rc = launch_timeblock(&d.buf[d.cur].p, n_dev_, &pb, &sp, &ho, d.main);
+        int rc = launch_timeblock(&d.buf[d.cur].p, n_kernel, &pb, &sp, &ho, d.main);
         if (rc != GLISSER_OK) throw CudaError(std::string("time-block launch failed: ") + timeblock_error());
         ck(cudaEventRecord(d.stop, d.main), "event");
-        int nxt = d.cur ^ 1;
-        rc = launch_partition(&d.buf[d.cur].p, &d.buf[nxt].p, n_dev_, d.d_scratch, d.d_ctr + 2, d.d_ctr + 3, d.main);
-        launches_total_ += 4;   // time block + count, scan, scatter
-        if (rc != GLISSER_OK) throw CudaError("partition launch failed");
-        ck(cudaMemcpyAsync(d.h_ctr, d.d_ctr, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, d.main), "counters");
-        ck(cudaMemcpyAsync(d.h_evals, d.d_evals, sizeof(unsigned long long), cudaMemcpyDeviceToHost, d.main), "evals");
-        ck(cudaEventRecord(d.done, d.main), "event");
-        d.cur = nxt;
-        host_dirty_ = true;
+        launches_total_ += 1;
+        // without encounter particles to bring back the partition follows the
+        // kernel directly; otherwise after SWIFT's results are in place
+        if (n_enc == 0) launch_partition_now();
     }
     // host work overlapped with the kernel
     auto c0 = clk::now();
-    snapshot_ = pl_;
-    t += cur_dt_ * (double)cur_tbsize_;
-    update_planets();
+    if (n_enc > 0) {
+        auto ce = clk::now();
+        handle_encounters(false, tm);
+        tm.enc = ms_since(ce);
+    } else {
+        auto cp = clk::now();
+        snapshot_ = pl_;
+        t += cur_dt_ * (double)cur_tbsize_;
+        update_planets();
+        tm.planet = ms_since(cp);
+    }
     double cpu = ms_since(c0);
-    if (prev_alive > 0) {
+    if (n_range > 0) {
+        auto cr = clk::now();
+        if (!partitioned) launch_partition_now();
         ck(cudaEventSynchronize(d.done), "block");
-        ck(cudaEventElapsedTime(&gpu, d.start, d.stop), "elapsed");
+        if (n_kernel > 0) ck(cudaEventElapsedTime(&gpu, d.start, d.stop), "elapsed");
         uint32_t status = d.h_ctr[1];
         if (status) throw CudaError("time-block kernel reported a planet-log staging timeout");
         uint32_t n0 = d.h_ctr[2], n1 = d.h_ctr[3];
         uint32_t k = std::min<uint32_t>(d.h_ctr[0], (uint32_t)std::max<size_t>(pa_.n, 1));
         evals_total_ += *d.h_evals;
         // both particle buffers must agree on the particles that left the
-        // alive range this block (the next partition reads only the alive one)
-        if (n0 + n1 < prev_alive) {
-            int rc = launch_copy_range(&d.buf[d.cur].p, &d.buf[d.cur ^ 1].p, n0 + n1, prev_alive, d.main);
+        // partitioned range this block (the next partition reads only one)
+        if (n0 + n1 < n_range) {
+            int rc = launch_copy_range(&d.buf[d.cur].p, &d.buf[d.cur ^ 1].p, n0 + n1, n_range, d.main);
             if (rc != GLISSER_OK) throw CudaError("copy launch failed");
             launches_total_ += 1;
         }
         // particles that kept their flags advanced the whole block; the
         // flagged ones add their deathtime index below
-        psteps_total_ += (unsigned long long)(prev_alive - std::min<size_t>(prev_alive, d.h_ctr[0])) *
-                         d.blk_len[used];
-        n_dev_ = cfg.resolve_encounters ? n0 : n0 + n1;
-        n_encounter_ = cfg.resolve_encounters ? n1 : 0;
+        psteps_total_ += (unsigned long long)(n_kernel - std::min<size_t>(n_kernel, d.h_ctr[0])) * d.blk_len[used];
+        n_dev_ = resolve ? n0 : n0 + n1;
+        n_encounter_ = resolve ? n1 : 0;
         flagged_.clear();
         if (k) {
+            auto cd = clk::now();
             ck(cudaMemcpyAsync(d.h_ho_id, d.d_ho_id, k * sizeof(uint32_t), cudaMemcpyDeviceToHost, d.main), "hand-off");
             ck(cudaMemcpyAsync(d.h_ho_dti, d.d_ho_dti, k * sizeof(uint32_t), cudaMemcpyDeviceToHost, d.main), "hand-off");
             ck(cudaMemcpyAsync(d.h_ho_flags, d.d_ho_flags, k * sizeof(uint16_t), cudaMemcpyDeviceToHost, d.main),
                "hand-off");
             ck(cudaStreamSynchronize(d.main), "hand-off sync");
+            tm.dl = ms_since(cd);
             for (uint32_t q = 0; q < k; q++) {
                 flagged_.push_back({ d.h_ho_id[q], d.h_ho_flags[q], d.h_ho_dti[q] });
                 psteps_total_ += d.h_ho_dti[q];
             }
-            std::sort(flagged_.begin(), flagged_.end(),
-                      [](const FlaggedEntry& a, const FlaggedEntry& b) { return a.id < b.id; });
-            float tf = (float)t;
-            for (auto& f : flagged_) {
-                set_deathtime(f.id, tf);
-                if ((f.flags & 0x04) && log)
-                    *log << "warning - particle " << f.id << " did not converge on GPU" << std::endl;
-                if (encounter_out) {
-                    *encounter_out << std::setprecision(17) << f.id << ((f.flags & 0x80) ? " death " : " encounter ")
-                                   << t << "\n";
-                }
+        }
+        // particles SWIFT removed this block leave the alive range with them
+        // (src/executor.cu:802-825 visits the whole range that left)
+        for (size_t q = 0; q < n_enc; q++)
+            if (enc_.flags[q] != 0) flagged_.push_back({ enc_.id[q], enc_.flags[q], enc_.dti[q] });
+        // particles that entered the first block already in an encounter kept
+        // their flag (the kernel reports only flags it changed)
+        for (const FlaggedEntry& f : initial_flagged_) flagged_.push_back(f);
+        initial_flagged_.clear();
+        std::sort(flagged_.begin(), flagged_.end(),
+                  [](const FlaggedEntry& a, const FlaggedEntry& b) { return a.id < b.id; });
+        float tf = (float)t;
+        for (auto& f : flagged_) {
+            set_deathtime(f.id, tf);
+            if ((f.flags & 0x04) && log)
+                *log << "warning - particle " << f.id << " did not converge on GPU" << std::endl;
+            if (encounter_out) {
+                *encounter_out << std::setprecision(17) << f.id << ((f.flags & 0x80) ? " death " : " encounter ") << t
+                               << "\n";
             }
         }
+        // at the end of a lookup interval the particles that entered an
+        // encounter in this block are brought to its end on SWIFT now, with
+        // the interval that closed (src/executor.cu:837-873)
+        if (resolve && starting_interval_ && n_encounter_ > 0) {
+            auto ce = clk::now();
+            handle_encounters(true, tm);
+            tm.enc2 = ms_since(ce);
+        }
+        tm.resync = ms_since(cr);
     }
+    tm.cpu = cpu;
+    tm.gpu = gpu;
+    tm.total = ms_since(t_total);
+    timing_ = tm;
+    if (timing_out) write_timing_row(tm, n_enc_start);
     if (cpu_ms) *cpu_ms = cpu;
     if (gpu_ms) *gpu_ms = gpu;
     return starting_interval_ || !cfg.resolve_encounters;
 }
 
+void Executor::EncounterSet::resize(size_t n)
+{
+    for (auto* a : { &rx, &ry, &rz, &vx, &vy, &vz, &ax, &ay, &az }) a->assign(n, 0.0);
+    id.assign(n, 0);
+    dti.assign(n, 0);
+    flags.assign(n, 0);
+}
+
+void Executor::fetch_encounters(int buf, size_t begin, size_t n)
+{
+    Impl& d = *d_;
+    enc_.resize(n);
+    if (n == 0) return;
+    const glisser_particles& p = d.buf[buf].p;
+    const double* src[6] = { p.rx, p.ry, p.rz, p.vx, p.vy, p.vz };
+    double* dst[6] = { enc_.rx.data(), enc_.ry.data(), enc_.rz.data(), enc_.vx.data(), enc_.vy.data(), enc_.vz.data() };
+    // the side stream reads the encounter range while the kernel may still
+    // be integrating the range before it
+    for (int c = 0; c < 6; c++)
+        ck(cudaMemcpyAsync(dst[c], src[c] + begin, n * sizeof(double), cudaMemcpyDeviceToHost, d.dth), "fetch");
+    ck(cudaMemcpyAsync(enc_.id.data(), p.id + begin, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, d.dth), "fetch");
+    ck(cudaMemcpyAsync(enc_.flags.data(), p.flags + begin, n * sizeof(uint16_t), cudaMemcpyDeviceToHost, d.dth),
+       "fetch");
+    ck(cudaStreamSynchronize(d.dth), "fetch sync");
+}
+
+void Executor::store_encounters(int buf, size_t begin, size_t n)
+{
+    Impl& d = *d_;
+    if (n == 0) return;
+    const glisser_particles& p = d.buf[buf].p;
+    double* dst[9] = { p.rx, p.ry, p.rz, p.vx, p.vy, p.vz, p.ax, p.ay, p.az };
+    const double* src[9] = { enc_.rx.data(), enc_.ry.data(), enc_.rz.data(), enc_.vx.data(), enc_.vy.data(),
+                             enc_.vz.data(), enc_.ax.data(), enc_.ay.data(), enc_.az.data() };
+    for (int c = 0; c < 9; c++)
+        ck(cudaMemcpyAsync(dst[c] + begin, src[c], n * sizeof(double), cudaMemcpyHostToDevice, d.main), "store");
+    ck(cudaMemcpyAsync(p.id + begin, enc_.id.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, d.main), "store");
+    ck(cudaMemcpyAsync(p.flags + begin, enc_.flags.data(), n * sizeof(uint16_t), cudaMemcpyHostToDevice, d.main),
+       "store");
+    ck(cudaMemcpyAsync(p.deathtime_index + begin, enc_.dti.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                       d.main),
+       "store");
+}
+
+void Executor::encounter_accelerations(size_t n)
+{
+    // helio_acc_particle (src/wh.cpp:611-657) at the last step of the block
+    // just integrated: h0 and the planet positions of that step (the old
+    // log's last record) with the live masses and encounter radii.  Its
+    // flags overwrite SWIFT's; a close-encounter flag is then cleared so that
+    // the next block detects the encounter itself (src/executor.cu:566-576).
+    const Planets& P = snapshot_;
+    const size_t npl_old = P.n_alive;
+    std::vector<double> pos(3 * (npl_old > 0 ? npl_old - 1 : 0));
+    for (size_t j = 1; j < npl_old; j++) {
+        pos[3 * (j - 1)] = P.r[j].x;
+        pos[3 * (j - 1) + 1] = P.r[j].y;
+        pos[3 * (j - 1) + 2] = P.r[j].z;
+    }
+    const Vec3 h0 = npl_old > 1 ? indirect_term(pos.data(), P.m, npl_old) : Vec3{ 0, 0, 0 };
+    const size_t npl = std::min(pl_.n_alive, npl_old);
+    const double outer2 = cfg.outer_radius * cfg.outer_radius;
+    const float tf = (float)t;
+    for (size_t k = 0; k < n; k++) {
+        const Vec3 r{ enc_.rx[k], enc_.ry[k], enc_.rz[k] };
+        Vec3 a = h0;
+        uint16_t fl = enc_.flags[k];
+        bool stamped = false;
+        for (size_t j = 1; j < npl; j++) {
+            Vec3 dr = r - P.r[j];
+            double r2 = dr.lensq();
+            double inv3 = 1. / (r2 * std::sqrt(r2));
+            double fac = pl_.m[j] * inv3;
+            a -= dr * fac;
+            if (r2 < rh_[j] * rh_[j]) {
+                stamped = true;
+                fl = (uint16_t)((j << 8) | 0x0001);
+            }
+        }
+        double r2 = r.lensq();
+        if (r2 < rh_[0] * rh_[0]) {
+            stamped = true;
+            fl = 0x0001;
+        }
+        if (r2 > outer2) {
+            stamped = true;
+            fl = 0x0002;
+        }
+        if (stamped) set_deathtime(enc_.id[k], tf);
+        if ((fl & 0xFF) == 0x01) fl = 0;
+        enc_.flags[k] = fl;
+        enc_.ax[k] = a.x;
+        enc_.ay[k] = a.y;
+        enc_.az[k] = a.z;
+        // the host's deathtime index travels back with the state; the
+        // reference never downloads it, so it is the zero it started with
+        enc_.dti[k] = 0;
+    }
+}
+
+void Executor::handle_encounters(bool from_resync, BlockTiming& tm)
+{
+    // Executor::handle_encounters (src/executor.cu:470-596).  Called in
+    // step_block while the kernel integrates the current block (SWIFT
+    // resumes the encounter particles from the start of the previous block
+    // to the end of the current one), or after the partition at the end of
+    // a lookup interval (from the start of the block just integrated to the
+    // interval's end).
+    Impl& d = *d_;
+    auto& ip = interp_;
+    const size_t begin = n_dev_;
+    const size_t n = n_encounter_;
+    const size_t prev_len = (starting_interval_ && !from_resync) ? 0 : prev_tbsize_;
+    const size_t cur_len = from_resync ? 0 : cur_tbsize_;
+    const double which_dt = from_resync ? prev_dt_ : cur_dt_;
+    if (from_resync && !(std::abs(ip.t0 - t) < 1e-2))
+        throw std::runtime_error("sanity check failed: end-of-chunk encounter time");
+    const double rel_t = from_resync ? ip.t0 - ip.t_m1 : ip.rel_t - ip.eff_dt * (double)cur_tbsize_;
+    const auto clocks = clk::now();
+    fetch_encounters(d.cur, begin, n);
+    std::vector<Vec3> r(n), v(n);
+    for (size_t k = 0; k < n; k++) {
+        r[k] = Vec3{ enc_.rx[k], enc_.ry[k], enc_.rz[k] };
+        v[k] = Vec3{ enc_.vx[k], enc_.vy[k], enc_.vz[k] };
+    }
+    // the lookup interval SWIFT integrates in: the current one, or at an
+    // interval boundary the one that just closed
+    SwiftHistory h;
+    h.m0 = pl_.m[0];
+    const std::vector<uint32_t>* planet_ids;
+    if (from_resync) {
+        const auto& o = ip.old;
+        h.span = ip.t0 - ip.t_m1;
+        h.npl = o.n_alive;
+        h.ids = o.ids.data(); h.mass = o.mass.data();
+        h.aei_i = o.aei_i.data(); h.oom_i = o.oom_i.data(); h.aei_f = o.aei_f.data(); h.oom_f = o.oom_f.data();
+        planet_ids = &o.ids;
+    } else {
+        h.span = ip.t1 - ip.t0;
+        h.npl = ip.n_alive;
+        h.ids = ip.ids.data(); h.mass = ip.mass.data();
+        h.aei_i = ip.aei_i.data(); h.oom_i = ip.oom_i.data(); h.aei_f = ip.aei_f.data(); h.oom_f = ip.oom_f.data();
+        planet_ids = &ip.ids;
+    }
+    double wswift = 0, iswift = 0, rswift = 0, dswift = 0;
+    swift_->begin(h, *planet_ids, n, r.data(), v.data(), rel_t, which_dt, prev_len, cur_len, &wswift, &iswift);
+    if (!from_resync) {
+        // the planets of the next block while SWIFT runs (outputs are written
+        // by the caller after step_block returns)
+        auto cp = clk::now();
+        try {
+            snapshot_ = pl_;
+            t += cur_dt_ * (double)cur_tbsize_;
+            update_planets();
+        } catch (...) {
+            swift_->reap();
+            throw;
+        }
+        tm.planet = ms_since(cp);
+    }
+    swift_->end(n, enc_.id.data(), r.data(), v.data(), enc_.flags.data(), &rswift, &dswift);
+    if (!from_resync) {
+        tm.wswift = wswift;
+        tm.iswift = iswift;
+        tm.rswift = rswift;
+        tm.dswift = dswift;
+        tm.swift = ms_since(clocks);
+    }
+    for (size_t k = 0; k < n; k++) {
+        if (!std::isfinite(r[k].x) || !std::isfinite(r[k].y) || !std::isfinite(r[k].z) || !std::isfinite(v[k].x) ||
+            !std::isfinite(v[k].y) || !std::isfinite(v[k].z))
+            throw std::runtime_error("SWIFT returned a non-finite state for particle " + std::to_string(enc_.id[k]));
+        enc_.rx[k] = r[k].x; enc_.ry[k] = r[k].y; enc_.rz[k] = r[k].z;
+        enc_.vx[k] = v[k].x; enc_.vy[k] = v[k].y; enc_.vz[k] = v[k].z;
+    }
+    encounter_accelerations(n);
+    auto cu = clk::now();
+    if (!from_resync) {
+        // into the range after the unflagged particles of the running
+        // kernel's buffer; the partition after the block sorts them in
+        store_encounters(d.cur, begin, n);
+    } else {
+        // sort the range here: unflagged, encounter, removed (the partial
+        // partitions of src/executor.cu:849-858); what follows it is removed
+        std::vector<size_t> order(n);
+        std::iota(order.begin(), order.end(), 0);
+        auto m1 = std::stable_partition(order.begin(), order.end(), [&](size_t q) { return enc_.flags[q] == 0; });
+        auto m2 = std::stable_partition(m1, order.end(), [&](size_t q) { return (enc_.flags[q] & 0xFE) == 0; });
+        const size_t n_ok = (size_t)(m1 - order.begin()), n_e = (size_t)(m2 - m1);
+        EncounterSet s = enc_;
+        for (size_t q = 0; q < n; q++) {
+            size_t o = order[q];
+            enc_.rx[q] = s.rx[o]; enc_.ry[q] = s.ry[o]; enc_.rz[q] = s.rz[o];
+            enc_.vx[q] = s.vx[o]; enc_.vy[q] = s.vy[o]; enc_.vz[q] = s.vz[o];
+            enc_.ax[q] = s.ax[o]; enc_.ay[q] = s.ay[o]; enc_.az[q] = s.az[o];
+            enc_.id[q] = s.id[o]; enc_.dti[q] = s.dti[o]; enc_.flags[q] = s.flags[o];
+        }
+        // both buffers: the removed ones lie outside the next partition's range
+        store_encounters(d.cur, begin, n);
+        store_encounters(d.cur ^ 1, begin, n);
+        n_dev_ = begin + n_ok;
+        n_encounter_ = n_e;
+        host_dirty_ = true;
+    }
+    ck(cudaStreamSynchronize(d.main), "store sync");
+    tm.encup = ms_since(cu);
+}
+
+void Executor::write_timing_header()
+{
+    *timing_out << "t,      n_enc,  enc,    wswift, iswift, swift,  rswift, dswift, io,     planet, planetu,encup,  "
+                   "sort,   dl,     endenc, resync, cpu,    gpu,    total"
+                << std::endl;
+}
+
+void Executor::write_timing_row(const BlockTiming& tm, size_t n_enc)
+{
+    std::ostream& o = *timing_out;
+    o << std::left << std::fixed << std::setprecision(3);
+    const double cols[19] = { t, (double)n_enc, tm.enc, tm.wswift, tm.iswift, tm.swift, tm.rswift,
+                              tm.dswift, tm.io, tm.planet, tm.planetu, tm.encup, tm.sort, tm.dl, tm.enc2,
+                              tm.resync, tm.cpu, tm.gpu, tm.total };
+    for (int c = 0; c < 19; c++) {
+        if (c == 1) o << std::setw(8) << (size_t)cols[c];
+        else o << std::setw(8) << cols[c];
+    }
+    o << std::endl;
+}
+
 void Executor::finish()
 {
+    // stat.out: SWIFT's status of every particle handed to it
+    // (src/executor.cu:880-882; empty when none was)
+    if (!cfg.outfolder.empty()) {
+        std::ofstream st(cfg.outfolder + "/stat.out");
+        if (swift_) swift_->stats.write(st);
+    }
     if (initialized_ && d_->device) {
         ck(cudaStreamSynchronize(d_->main), "finish");
         download_particles();

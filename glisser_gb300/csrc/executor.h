@@ -13,11 +13,18 @@
 #include "config.h"
 #include "planets.h"
 #include "state_io.h"
+#include "swift.h"
 
 namespace glisser {
 
 struct CudaError : std::runtime_error {
     using std::runtime_error::runtime_error;
+};
+
+// Per-block timings in ms, the columns of timing.out (src/executor.cu:715-735).
+struct BlockTiming {
+    double enc = 0, wswift = 0, iswift = 0, swift = 0, rswift = 0, dswift = 0, io = 0, planet = 0, planetu = 0,
+           encup = 0, sort = 0, dl = 0, enc2 = 0, resync = 0, cpu = 0, gpu = 0, total = 0;
 };
 
 struct FlaggedEntry {
@@ -82,6 +89,10 @@ public:
 
     std::ostream* log = nullptr;             // progress / warnings (stdout tee)
     std::ostream* encounter_out = nullptr;   // encounter.out
+    std::ostream* timing_out = nullptr;      // timing.out: header at init, one row per block
+    const BlockTiming& last_timing() const { return timing_; }
+    // SWIFT's status arrays of the particles handed to it (Resolve-Encounters)
+    const SwiftStats* swift_stats() const { return swift_ ? &swift_->stats : nullptr; }
 
 private:
     Planets pl_;            // live planets (one block ahead of the particles after init)
@@ -111,6 +122,26 @@ private:
 
     size_t n_dev_ = 0, n_encounter_ = 0;
     std::vector<FlaggedEntry> flagged_;
+    BlockTiming timing_;
+
+    // Resolve-Encounters: the SWIFT runner and the encounter particles in
+    // transit (structure of arrays, as the device holds them)
+    std::unique_ptr<SwiftRunner> swift_;
+    struct EncounterSet {
+        std::vector<double> rx, ry, rz, vx, vy, vz, ax, ay, az;
+        std::vector<uint32_t> id, dti;
+        std::vector<uint16_t> flags;
+        void resize(size_t n);
+    } enc_;
+    void handle_encounters(bool from_resync, BlockTiming& tm);
+    void fetch_encounters(int buf, size_t begin, size_t n);
+    void store_encounters(int buf, size_t begin, size_t n);
+    void encounter_accelerations(size_t n);
+    void write_timing_row(const BlockTiming& tm, size_t n_enc);
+    void write_timing_header();
+    // encounter-flagged particles of the initial state (reported after the
+    // first block, as the reference's resync reports them)
+    std::vector<FlaggedEntry> initial_flagged_;
 
     struct Impl;
     std::unique_ptr<Impl> d_;

@@ -230,9 +230,10 @@ void HistoryInterpolator::open(const std::string& path, size_t max_planets, doub
     aei0_.assign(cap_, Vec3{ 0, 0, 0 });
     aei1_ = oom0_ = oom1_ = aei0_;
     m1_.assign(cap_, 0.0);
-    aei_i = daei = oom_i = doom = aei0_;
+    aei_i = daei = oom_i = doom = aei_f = oom_f = aei0_;
     ids.assign(cap_, 0);
     mass.assign(cap_, 0.0);
+    old = Interval{ ids, mass, aei_i, oom_i, aei_f, oom_f, 0 };
     t0 = std::numeric_limits<double>::infinity();
     t1 = read_le<double>(in_);
     t_m1 = std::numeric_limits<double>::quiet_NaN();
@@ -265,6 +266,7 @@ void HistoryInterpolator::open(const std::string& path, size_t max_planets, doub
 void HistoryInterpolator::next(Planets& p)
 {
     t_m1 = t0;
+    old = Interval{ ids, mass, aei_i, oom_i, aei_f, oom_f, n_alive };
     aei0_ = aei1_;
     oom0_ = oom1_;
     t0 = t1;
@@ -293,6 +295,8 @@ void HistoryInterpolator::next(Planets& p)
         mass[k] = m1_[s];
         aei_i[k] = aei0_[s];
         oom_i[k] = oom0_[s];
+        aei_f[k] = aei1_[s];
+        oom_f[k] = oom1_[s];
         daei[k] = (aei1_[s] - aei0_[s]) / span;
         Vec3 d = oom1_[s] - oom0_[s];
         if (d.x > PI) d.x -= 2 * PI;

@@ -95,6 +95,18 @@ public:
     std::vector<Vec3> aei_i, daei, oom_i, doom;
     std::vector<uint32_t> ids;
     std::vector<double> mass;
+    // the interval's end elements (reduced_aei_f / reduced_oom_f)
+    std::vector<Vec3> aei_f, oom_f;
+    // The previous interval's planets (the reduced_*_old arrays and
+    // n_alive_old of src/interp.cpp:178-188), which the SWIFT hand-off at an
+    // interval boundary integrates with.  Arrays keep the full capacity, as
+    // the current ones do.
+    struct Interval {
+        std::vector<uint32_t> ids;
+        std::vector<double> mass;
+        std::vector<Vec3> aei_i, oom_i, aei_f, oom_f;
+        size_t n_alive = 0;
+    } old;
 
 private:
     std::ifstream in_;

@@ -254,9 +254,16 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
         const uint32_t i = first + off;
         const bool active = off < count;
         if (active) {
-            if (p.kill && (flags[k] & 0x01)) flags[k] = (uint16_t)((flags[k] & 0xFF00) | 0x80);
-            p.pa.rx[i] = rx[k]; p.pa.ry[i] = ry[k]; p.pa.rz[i] = rz[k];
-            p.pa.vx[i] = vx[k]; p.pa.vy[i] = vy[k]; p.pa.vz[i] = vz[k];
+            if (p.kill == GLISSER_ENCOUNTERS_KILL && (flags[k] & 0x01))
+                flags[k] = (uint16_t)((flags[k] & 0xFF00) | 0x80);
+            // a rolled-back encounter particle leaves its block-start state in
+            // place (nothing has overwritten it yet)
+            const bool rollback =
+                p.kill == GLISSER_ENCOUNTERS_ROLLBACK && flags[k] != 0 && (flags[k] & 0xFE) == 0;
+            if (!rollback) {
+                p.pa.rx[i] = rx[k]; p.pa.ry[i] = ry[k]; p.pa.rz[i] = rz[k];
+                p.pa.vx[i] = vx[k]; p.pa.vy[i] = vy[k]; p.pa.vz[i] = vz[k];
+            }
             p.pa.ax[i] = ax[k]; p.pa.ay[i] = ay[k]; p.pa.az[i] = az[k];
             p.pa.flags[i] = flags[k];
             p.pa.deathtime_index[i] = dti[k];

@@ -59,6 +59,8 @@ int launch_timeblock(const glisser_particles* pa, size_t n_alive, const glisser_
     if (!handoff_ok(ho)) return GLISSER_E_INVALID;
     if (!(sp->dt > 0) || !(sp->outer_radius >= 0)) return GLISSER_E_INVALID;
     if (!(sp->kepler_tol == 0 || (sp->kepler_tol >= 1e-16 && sp->kepler_tol <= 1e-8))) return GLISSER_E_INVALID;
+    if (sp->kill_encounters < GLISSER_ENCOUNTERS_KEEP || sp->kill_encounters > GLISSER_ENCOUNTERS_ROLLBACK)
+        return GLISSER_E_INVALID;
     if (pl->len > 0) {
         if (!pl->log || !pl->m || !pl->id || !pl->rh) return GLISSER_E_INVALID;
         if (((uintptr_t)pl->log & 15u) != 0) return GLISSER_E_INVALID;

@@ -51,6 +51,14 @@ extern "C" {
 #define GLISSER_STARTER_SERIES 1   /* tenth-order time series / FP32 Kepler pre-solve */
 #define GLISSER_STARTER_LEARNED 2  /* MLP initial guess, classic fallback */
 
+/* What the time-block kernel does with a particle that ends the block in a
+ * close encounter (flags != 0, (flags & 0xFE) == 0), glisser_step_params
+ * .kill_encounters. */
+#define GLISSER_ENCOUNTERS_KEEP 0      /* keeps the flag and the state of the flag step */
+#define GLISSER_ENCOUNTERS_KILL 1      /* 0x01 -> 0x80 (KillEncounterKernel, src/executor.cu:63-77) */
+#define GLISSER_ENCOUNTERS_ROLLBACK 2  /* keeps the flag and its block-start r, v: the rollback state the
+                                          SWIFT hand-off resumes from (src/executor.cu:624-633, 827-834) */
+
 /* Feature normalisation and training box of a learned starter (features
  * f0 = log(tau), tau = dt sqrt(mu/r0^3), f1 = r0.v0 / sqrt(mu r0),
  * f2 = alpha r0 / mu; output z = log(s r0 / dt) / tau).  Element 3 of each
@@ -97,7 +105,7 @@ typedef struct glisser_step_params {
     double dt;
     double outer_radius;         /* Outer-Limit */
     int32_t starter;             /* GLISSER_STARTER_* */
-    int32_t kill_encounters;     /* nonzero: 0x01 -> 0x80 at block end (KillEncounterKernel) */
+    int32_t kill_encounters;     /* GLISSER_ENCOUNTERS_*: what a particle flagged 0x01 keeps */
     const void *mlp;             /* learned-starter weights (device), or NULL */
     double kepler_tol;           /* Kepler residual tolerance |f| < tol*dt; 0 = 1e-13 (the reference's DANBYB) */
 } glisser_step_params;
@@ -231,7 +239,8 @@ int glisser_get_planets(const glisser_t *h, double *m, double *r, double *v, uin
  * records of 64 vectors at most; *npl and *len receive the block's shape. */
 int glisser_get_planet_block(const glisser_t *h, double *log, double *m, uint32_t *id, double *rh, uint32_t cap_steps,
                              uint32_t *npl, uint32_t *len);
-/* The particles flagged in the last block (the compacted hand-off list). */
+/* The particles flagged in the last block (the compacted hand-off list),
+ * with Resolve-Encounters also those SWIFT removed in it (deathtime index 0). */
 int glisser_get_flagged(const glisser_t *h, uint32_t *ids, uint16_t *flags, uint32_t *deathtime_index,
                         size_t cap, size_t *n);
 
@@ -240,6 +249,50 @@ int glisser_get_flagged(const glisser_t *h, uint32_t *ids, uint16_t *flags, uint
 int glisser_write_state(const glisser_t *h, const char *path, int binary);
 int glisser_write_track(const glisser_t *h, const char *path, int append);
 int glisser_write_plhist(const glisser_t *h, const char *path, int begin);
+
+/* stat.out of the run (SwiftEncounterIntegrator::write_stat,
+ * src/swift.cpp:274-290): SWIFT's status arrays of every particle handed to
+ * it with Resolve-Encounters, in ascending id order (empty otherwise).
+ * glisser_finish also writes it as <Output-Folder>/stat.out. */
+int glisser_write_stat(const glisser_t *h, const char *path);
+
+/* ---- SWIFT encounter hand-off protocol (src/swift.cpp:44-460) ----------
+ * With Resolve-Encounters 1 the executor runs Swift-Path itself over the
+ * particles that entered a close encounter: the time-block kernel leaves
+ * their block-start state in place (GLISSER_ENCOUNTERS_ROLLBACK), SWIFT
+ * resumes them from there while the next block integrates, and they rejoin
+ * the block integrator at the partition after it.  These calls expose the same files to a host that resolves encounters with
+ * its own program, from glisser_get_flagged's hand-off list.  All vectors
+ * are [n][3]; files are byte-identical to the reference's.
+ *
+ * write_param_in: SWIFT integrates from rel_t - prev_len * dt to
+ * rel_t + cur_len * dt (relative to the lookup interval's start). */
+int glisser_swift_write_param(const char *path, double rel_t, size_t prev_len, size_t cur_len, double dt,
+                              double outer_radius);
+/* write_tp_in: n test particles with statlen zeroed status entries. */
+int glisser_swift_write_tp(const char *path, size_t n, const double *r, const double *v, uint32_t statlen);
+/* write_planetary_history: one lookup interval of span time units as a
+ * two-record history -- the npl planets present at both ends (ids, masses
+ * G*m) with their (a, e, i) and (Omega, omega, M) at the start (aei_i,
+ * oom_i) and at the end (aei_f, oom_f); m0 = G * solar mass. */
+int glisser_swift_write_history(const char *path, double m0, double span, size_t npl, const uint32_t *ids,
+                                const double *mass, const double *aei_i, const double *oom_i, const double *aei_f,
+                                const double *oom_f);
+/* SWIFT's per-particle status arrays accumulated over hand-offs (statmap,
+ * istat, rstat of src/swift.h:47-51). */
+typedef struct glisser_swift_stats glisser_swift_stats;
+int glisser_swift_stats_create(uint32_t statlen, glisser_swift_stats **out);
+int glisser_swift_stats_destroy(glisser_swift_stats *s);
+/* end_integrate's reading of one output file (src/swift.cpp:150-272): n
+ * particles with ids; r, v, flags receive the returned state and deathflags
+ * (0 alive; 0x04, 0x02, 0x80, or planet id << 8 | 0x80 removed).  planet_ids
+ * lists the interval's planets in SWIFT's numbering order (planet 2 first).
+ * Returns GLISSER_E_RUNTIME on a count mismatch or a malformed file. */
+int glisser_swift_read_tpout(glisser_swift_stats *s, const char *path, size_t n, const uint32_t *ids,
+                             const uint32_t *planet_ids, size_t n_planet_ids, double *r, double *v, uint16_t *flags);
+/* istat / rstat [statlen] of particle id; GLISSER_E_INVALID if it has none. */
+int glisser_swift_stats_get(const glisser_swift_stats *s, uint32_t id, int32_t *istat, double *rstat);
+int glisser_swift_write_stat(const glisser_swift_stats *s, const char *path);
 
 /* Selects the Kepler starter (default GLISSER_STARTER_SERIES) and, for the
  * learned starter, the weights blob written by glisser_mlp_save. */

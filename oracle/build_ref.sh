@@ -22,7 +22,7 @@ mkdir -p "$OUT"
 INCS="-include limits -include string -include cstring -include array -include map -include cmath -include stdexcept -include algorithm"
 FLAGS="-O2 -fPIC -ffp-contract=off -DNO_CUDA -w"
 pids=()
-for f in wh convert data interp util; do
+for f in wh convert data interp util swift; do
     g++ -std=c++11 $FLAGS $INCS -c "$REF/src/$f.cpp" -o "$OUT/$f.o" &
     pids+=($!)
 done

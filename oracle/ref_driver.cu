@@ -7,17 +7,24 @@
 // The particle kernel arithmetic is the reference's own
 // MVSKernel::step_forward (src/wh.cu:113-177), which is __host__ __device__:
 // including src/wh.cu in this host translation unit runs exactly that code on
-// the CPU.  The block loop below restates the no-encounter-resolution branch of
-// Executor::init / update_planets / loop / resync2 (src/executor.cu:85-217,
-// 226-320, 598-764, 766-877) on top of the reference's WHIntegrator
-// (src/wh.cpp) and Interpolator (src/interp.cpp).
+// the CPU.  The block loop below restates Executor::init / update_planets /
+// loop / resync2 / handle_encounters (src/executor.cu:85-217, 226-320,
+// 470-596, 598-764, 766-877) on top of the reference's WHIntegrator
+// (src/wh.cpp), Interpolator (src/interp.cpp) and, with Resolve-Encounters,
+// SwiftEncounterIntegrator (src/swift.cpp), which runs Swift-Path itself.
+// One set of particle arrays stands for both the device arrays and the host
+// mirror; where the two differ in the reference (the rollback state the host
+// reads back, the host's never-downloaded deathtime index) the emulation
+// says so.
 
 #include "wh.cu"
 #include "interp.h"
 #include "convert.h"
 #include "data.h"
+#include "swift.h"
 
 #include <algorithm>
+#include <iomanip>
 #include <cstring>
 #include <fstream>
 #include <numeric>
@@ -51,6 +58,23 @@ namespace
 		size_t dev_n_alive = 0;
 		std::string err;
 		std::ostringstream log;
+
+		// Resolve-Encounters: the encounter integrator, the rollback state
+		// (r, v in device order), the presort boundary, and a record of every
+		// hand-off for the tests
+		sr::swift::SwiftEncounterIntegrator swift;
+		Vf64_3 rb_r, rb_v;
+		size_t presort = 0;
+		struct SwiftCall
+		{
+			int old;
+			double t, rel_t, dt;
+			size_t prev_len, cur_len, begin, n;
+			Vu32 ids;
+			Vf64_3 r_in, v_in, r_out, v_out;
+			Vu16 flags_out;
+		};
+		std::vector<SwiftCall> calls;
 	};
 
 	void upload_planets(RefExec& e)
@@ -99,6 +123,142 @@ namespace
 		e.hd.planets.swap_logs();
 		e.integ.swap_logs();
 		upload_planets(e);
+	}
+
+	// stable partition of [begin, end) by pred, moving every per-particle
+	// array the reference's device partition moves
+	template<typename P>
+	size_t partition_all(RefExec& e, size_t begin, size_t end, P pred)
+	{
+		auto& pa = e.hd.particles;
+		if (end <= begin) return begin;
+		Vs idx(end - begin);
+		std::iota(idx.begin(), idx.end(), 0);
+		auto mid = std::stable_partition(idx.begin(), idx.end(), [&](size_t k) { return pred(pa.deathflags()[begin + k]); });
+		size_t boundary = begin + static_cast<size_t>(mid - idx.begin());
+		pa.gather(idx, begin, end - begin);
+		gather(pa.deathtime_index(), idx, begin, end - begin);
+		gather(e.dev_a, idx, begin, end - begin);
+		gather(e.rb_r, idx, begin, end - begin);
+		gather(e.rb_v, idx, begin, end - begin);
+		return boundary;
+	}
+
+	bool unflagged(uint16_t f) { return f == 0; }
+	bool alive(uint16_t f) { return (f & 0x00FE) == 0; }
+
+	// Executor::handle_encounters (src/executor.cu:470-596)
+	void handle_encounters(RefExec& e, bool called_from_resync)
+	{
+		auto& pa = e.hd.particles;
+		auto& ip = e.interp;
+		size_t encounter_start = pa.n_alive() - pa.n_encounter();
+		size_t prev_len = e.prev_tbsize;
+		if (e.starting_lookup_interval && !called_from_resync) prev_len = 0;
+		size_t cur_len = called_from_resync ? 0 : e.cur_tbsize;
+		double which_dt = called_from_resync ? e.prev_dt : e.cur_dt;
+		if (called_from_resync && !(std::abs(ip.t0 - e.t) < 1e-2)) throw std::runtime_error("end-of-chunk encounter time");
+		double rel_t = called_from_resync ? ip.t0 - ip.t_m1 : ip.rel_t - ip.eff_dt * static_cast<double>(e.cur_tbsize);
+		double which_t = called_from_resync ? ip.t0 : ip.t0 + rel_t;
+
+		RefExec::SwiftCall call;
+		call.old = called_from_resync ? 1 : 0;
+		call.t = which_t; call.rel_t = rel_t; call.dt = which_dt;
+		call.prev_len = prev_len; call.cur_len = cur_len;
+		call.begin = encounter_start; call.n = pa.n_encounter();
+		for (size_t i = encounter_start; i < encounter_start + call.n; i++)
+		{
+			call.ids.push_back(pa.id()[i]);
+			call.r_in.push_back(pa.r()[i]);
+			call.v_in.push_back(pa.v()[i]);
+		}
+
+		e.swift.begin_integrate(e.hd.planets, pa, ip, called_from_resync, which_t, rel_t, which_dt, prev_len, cur_len);
+		if (!called_from_resync)
+		{
+			e.hd.planets_snapshot = e.hd.planets.base;
+			e.t += e.cur_dt * static_cast<double>(e.cur_tbsize);
+			update_planets(e);
+		}
+		e.swift.end_integrate(pa);
+		for (size_t i = encounter_start; i < encounter_start + call.n; i++)
+		{
+			call.r_out.push_back(pa.r()[i]);
+			call.v_out.push_back(pa.v()[i]);
+			call.flags_out.push_back(pa.deathflags()[i]);
+		}
+		e.calls.push_back(call);
+
+		e.integ.helio_acc_particles(e.hd.planets, pa, encounter_start, pa.n_encounter(), e.t,
+			e.hd.planets.r_log().len_old - 1, true);
+		for (size_t i = encounter_start; i < encounter_start + pa.n_encounter(); i++)
+		{
+			if ((pa.deathflags()[i] & 0xFF) == 0x01) pa.deathflags()[i] = 0;
+			// upload_data: the host's deathtime index, never downloaded, is zero
+			pa.deathtime_index()[i] = 0;
+			e.dev_a[i] = e.integ.particle_a[i];
+		}
+		e.dev_n_alive = pa.n_alive();
+	}
+
+	// Executor::resync2 (src/executor.cu:766-877) with Resolve-Encounters
+	void resync_resolve(RefExec& e)
+	{
+		auto& pa = e.hd.particles;
+		size_t prev_alive = e.dev_n_alive;
+		e.dev_n_alive = partition_all(e, e.presort, prev_alive, unflagged);
+		pa.n_encounter() = partition_all(e, e.dev_n_alive, prev_alive, alive) - e.dev_n_alive;
+		pa.n_alive() = e.dev_n_alive + pa.n_encounter();
+		for (size_t i = e.dev_n_alive; i < prev_alive; i++)
+		{
+			pa.deathtime_map()[pa.id()[i]] = static_cast<float>(e.t);
+			e.log << pa.id()[i] << ((pa.deathflags()[i] & 0x80) ? " death " : " encounter ") << e.t << "\n";
+		}
+		// the host reads the encounter particles' rollback state
+		for (size_t i = e.dev_n_alive; i < e.dev_n_alive + pa.n_encounter(); i++)
+		{
+			pa.r()[i] = e.rb_r[i];
+			pa.v()[i] = e.rb_v[i];
+		}
+		if (e.starting_lookup_interval && pa.n_encounter() > 0)
+		{
+			size_t n_encounters = pa.n_encounter();
+			handle_encounters(e, true);
+			e.dev_n_alive = partition_all(e, e.dev_n_alive - n_encounters, e.dev_n_alive, unflagged);
+			pa.n_encounter() = partition_all(e, e.dev_n_alive, prev_alive, alive) - e.dev_n_alive;
+			pa.n_alive() = e.dev_n_alive + pa.n_encounter();
+		}
+	}
+
+	// Executor::loop (src/executor.cu:598-764) with Resolve-Encounters
+	void loop_resolve(RefExec& e)
+	{
+		auto& pa = e.hd.particles;
+		if (e.dev_n_alive > 0)
+		{
+			e.rb_r = pa.r();
+			e.rb_v = pa.v();
+			for (size_t i = 0; i < e.dev_n_alive; i++)
+			{
+				uint32_t d = 0;
+				sr::wh::MVSKernel::step_forward(pa.r()[i], pa.v()[i], pa.deathflags()[i], e.dev_a[i], d,
+					e.dev_len, e.dev_npl, e.dev_h0_log.data(), e.dev_r_log.data(), e.dev_m.data(),
+					e.dev_id.data(), e.dev_rh.data(), e.config.outer_radius, e.cur_dt, e.dev_m[0]);
+				pa.deathtime_index()[i] = d;
+			}
+			e.presort = partition_all(e, 0, e.dev_n_alive, unflagged);
+		}
+		if (pa.n_encounter() > 0)
+		{
+			handle_encounters(e, false);
+		}
+		else
+		{
+			e.hd.planets_snapshot = e.hd.planets.base;
+			e.t += e.cur_dt * static_cast<double>(e.cur_tbsize);
+			update_planets(e);
+		}
+		if (e.dev_n_alive > 0) resync_resolve(e);
 	}
 }
 
@@ -200,6 +360,10 @@ extern "C"
 			e.hd.particles.stable_partition_alive(na, e.hd.particles.n() - na);
 			e.dev_a = e.integ.particle_a;
 			e.dev_n_alive = e.hd.particles.n_alive();
+			e.swift = sr::swift::SwiftEncounterIntegrator(e.config, e.hd.particles.n());
+			e.log << std::setprecision(17);   // as Executor::init sets encounter.out
+			e.rb_r = e.hd.particles.r();
+			e.rb_v = e.hd.particles.v();
 			e.hd.planets_snapshot = e.hd.planets.base;
 			update_planets(e);
 		}
@@ -211,12 +375,17 @@ extern "C"
 		return 0;
 	}
 
-	// One block of Executor::loop without encounter resolution.
+	// One block of Executor::loop.
 	int ref_exec_loop(void* h)
 	{
 		RefExec& e = *static_cast<RefExec*>(h);
 		try
 		{
+			if (e.config.resolve_encounters)
+			{
+				loop_resolve(e);
+				return 0;
+			}
 			auto& pa = e.hd.particles;
 			size_t prev_alive = e.dev_n_alive;
 			size_t presort = 0;
@@ -282,6 +451,50 @@ extern "C"
 	}
 
 	const char* ref_exec_error(void* h) { return static_cast<RefExec*>(h)->err.c_str(); }
+
+	// The SWIFT hand-offs made so far: count, then per call its arguments
+	// (old-interval flag, t, rel_t, dt, prev/cur block lengths, first index,
+	// particle count) and data (ids, state handed over, state and flags
+	// end_integrate read back, all [n][3] / [n]).
+	size_t ref_exec_swift_calls(void* h) { return static_cast<RefExec*>(h)->calls.size(); }
+
+	void ref_exec_swift_call(void* h, size_t k, int* old, double* t3, size_t* sizes4)
+	{
+		const auto& c = static_cast<RefExec*>(h)->calls.at(k);
+		*old = c.old;
+		t3[0] = c.t; t3[1] = c.rel_t; t3[2] = c.dt;
+		sizes4[0] = c.prev_len; sizes4[1] = c.cur_len; sizes4[2] = c.begin; sizes4[3] = c.n;
+	}
+
+	void ref_exec_swift_call_data(void* h, size_t k, uint32_t* ids, double* r_in, double* v_in, double* r_out,
+		double* v_out, uint16_t* flags_out)
+	{
+		const auto& c = static_cast<RefExec*>(h)->calls.at(k);
+		for (size_t i = 0; i < c.n; i++)
+		{
+			ids[i] = c.ids[i];
+			flags_out[i] = c.flags_out[i];
+			const f64_3* src[4] = { &c.r_in[i], &c.v_in[i], &c.r_out[i], &c.v_out[i] };
+			double* dst[4] = { r_in, v_in, r_out, v_out };
+			for (int q = 0; q < 4; q++)
+			{
+				dst[q][3 * i] = src[q]->x; dst[q][3 * i + 1] = src[q]->y; dst[q][3 * i + 2] = src[q]->z;
+			}
+		}
+	}
+
+	// stat.out as Executor::finish writes it (src/executor.cu:880-882)
+	void ref_exec_write_stat(void* h, const char* path) { static_cast<RefExec*>(h)->swift.write_stat(path); }
+
+	// counts in the reference's own terms: device n_alive, host n_alive
+	// (alive + encounter), n_encounter
+	void ref_exec_counts2(void* h, size_t* dev_alive, size_t* host_alive, size_t* n_encounter)
+	{
+		RefExec& e = *static_cast<RefExec*>(h);
+		*dev_alive = e.dev_n_alive;
+		*host_alive = e.hd.particles.n_alive();
+		*n_encounter = e.hd.particles.n_encounter();
+	}
 
 	// encounter.out lines accumulated so far
 	size_t ref_exec_encounter_log(void* h, char* buf, size_t cap)

@@ -362,9 +362,111 @@ def main():
     print("wrote format fixtures")
 
 
+ENCOUNTER_CONFIG = ["Time-Step 0.2", "Time-Block-Size 50", "Final-Time 1e9", "Read-Planet-History 1",
+                    "Encounter-RH-Factor 3", "Cull-Radius 0.5", "Resolve-Encounters 1", "Swift-Process-Count 2",
+                    "Swift-Process-Min-Particle-Count 3"]
+
+
+def encounter_config(plh, swift, out):
+    return "\n".join(ENCOUNTER_CONFIG + ["Planet-History-File " + plh, "Swift-Path " + swift,
+                                         "Output-Folder " + out])
+
+
+def encounter_particles(L, n=600, seed=21):
+    """Particles on near-circular orbits across Neptune's in plhist_yr.bin."""
+    m, _ = synth.neptune_planets(synth.GM_SUN_AU_YR, a=30.4)
+    rng = np.random.default_rng(seed)
+    el = synth.particle_elements(rng, n, (28, 33), (0.0, 0.1), 5.0)
+    return cartesian(L, m[0], el)
+
+
+def gen_encounters(L, nblocks=24):
+    """Resolve-Encounters: the reference's own hand-off
+    (SwiftEncounterIntegrator, src/swift.cpp) under the restated executor loop,
+    with SWIFT stood in for by tests/fake_swift.py.  Records every block's
+    counts, the final state, encounter.out, stat.out, each hand-off's
+    arguments and data, and the files of every SWIFT call."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import fake_swift
+    wdir = tempfile.mkdtemp(prefix="glisser_enc_")
+    swift = fake_swift.wrapper(wdir)
+    arch = os.path.join(wdir, "archive")
+    os.environ["FAKE_SWIFT_ARCHIVE"] = arch
+    out = os.path.join(wdir, "out")
+    os.makedirs(out)
+    plh = os.path.join(HERE, "plhist_yr.bin")
+    m, _ = synth.neptune_planets(synth.GM_SUN_AU_YR, a=30.4)
+    m = np.array([m[0], 1e-24, m[1]])
+    pl_r = np.zeros((3, 3)); pl_v = np.zeros((3, 3))
+    pl_r[1, 0] = 5.2; pl_r[2, 0] = 30.4   # replaced by the history's first record
+    r, v = encounter_particles(L)
+    state = os.path.join(wdir, "enc.state.in")
+    cfg = encounter_config(plh, swift, out)
+    # particles that start inside an encounter radius would be flagged at init
+    # (and the reference leaves their accelerations in load order): leave them out
+    write_state(state, m, pl_r, pl_v, r, v)
+    run = RefRun(L, cfg + "\nInput-File " + state + "\n")
+    f0 = run.particles()["flags"]
+    keep = np.sort(run.particles()["id"][f0 == 0])
+    r, v = r[keep], v[keep]
+    ids = keep.astype(np.uint32)
+    write_state(state, m, pl_r, pl_v, r, v, ids=ids)
+    run = RefRun(L, cfg + "\nInput-File " + state + "\n")
+    L.ref_exec_counts2.argtypes = [C.c_void_p] + [C.POINTER(C.c_size_t)] * 3
+    L.ref_exec_swift_calls.argtypes = [C.c_void_p]
+    L.ref_exec_swift_calls.restype = C.c_size_t
+    L.ref_exec_swift_call.argtypes = [C.c_void_p, C.c_size_t, C.POINTER(C.c_int), D, C.POINTER(C.c_size_t)]
+    L.ref_exec_swift_call_data.argtypes = [C.c_void_p, C.c_size_t, U32, D, D, D, D, U16]
+    L.ref_exec_write_stat.argtypes = [C.c_void_p, C.c_char_p]
+    rec = dict(pl_m=m, pl_r=pl_r, pl_v=pl_v, r0=r, v0=v, id0=ids, nblocks=np.array(nblocks),
+               config=np.array("\n".join(ENCOUNTER_CONFIG)))
+    counts = []
+    for b in range(nblocks):
+        run.loop()
+        da, ha, ne = C.c_size_t(), C.c_size_t(), C.c_size_t()
+        L.ref_exec_counts2(run.h, C.byref(da), C.byref(ha), C.byref(ne))
+        counts.append((run.counts()[2], da.value, ha.value, ne.value))
+    rec["counts"] = np.array(counts)
+    st = run.particles()
+    for k in ("r", "v", "id", "flags", "deathtime"):
+        rec["out_" + k] = st[k]
+    rec["encounter_log"] = np.array(run.encounter_log())
+    stat = os.path.join(wdir, "stat.out")
+    L.ref_exec_write_stat(run.h, stat.encode())
+    rec["stat_out"] = np.array(open(stat).read())
+    ncall = L.ref_exec_swift_calls(run.h)
+    meta = np.zeros((ncall, 8))
+    for k in range(ncall):
+        old = C.c_int(); t3 = np.zeros(3); sz = (C.c_size_t * 4)()
+        L.ref_exec_swift_call(run.h, k, C.byref(old), p(t3, D), sz)
+        meta[k] = (old.value, *t3, *list(sz))
+        n = sz[3]
+        ids_k = np.zeros(n, np.uint32); fl = np.zeros(n, np.uint16)
+        arrs = [np.zeros((n, 3)) for _ in range(4)]
+        L.ref_exec_swift_call_data(run.h, k, p(ids_k, U32), *[p(a, D) for a in arrs], p(fl, U16))
+        rec["call%d_ids" % k] = ids_k
+        for nm, a in zip(("r_in", "v_in", "r_out", "v_out"), arrs):
+            rec["call%d_%s" % (k, nm)] = a
+        rec["call%d_flags" % k] = fl
+    rec["calls"] = meta   # old, t, rel_t, dt, prev_len, cur_len, begin, n
+    names = sorted(os.listdir(arch))
+    rec["archive_names"] = np.array(names)
+    for nm in names:
+        for tag in ("param", "hist", "tp", "tpout"):
+            with open(os.path.join(arch, nm, tag), "rb") as f:
+                rec["arch_%s_%s" % (nm, tag)] = np.frombuffer(f.read(), np.uint8)
+    np.savez_compressed(os.path.join(HERE, "encounters_t50.npz"), **rec)
+    del os.environ["FAKE_SWIFT_ARCHIVE"]
+    print("wrote encounters_t50.npz: %d particles, %d hand-offs, %d SWIFT calls; counts per block:"
+          % (len(ids), ncall, len(names)), [tuple(int(x) for x in c[1:]) for c in counts])
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["threebody"]:
         gen_threebody(ref())
+    elif sys.argv[1:] == ["encounters"]:
+        gen_encounters(ref())
     else:
         main()
         gen_threebody(ref())
+        gen_encounters(ref())

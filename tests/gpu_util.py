@@ -72,10 +72,12 @@ class DevHandoff:
                     flags=self.flags[:k].cpu().numpy().view(np.uint16), dti=self.dti[:k].cpu().numpy().view(np.uint32))
 
 
-def timeblock(parts, blk, dt, outer, starter=G.STARTER_SERIES, kill=True, handoff=None, mlp=0):
+def timeblock(parts, blk, dt, outer, starter=G.STARTER_SERIES, kill=True, handoff=None, mlp=0, encounters=None):
+    """One block through the C ABI; `encounters` (G.ENCOUNTERS_*) overrides `kill`."""
     ho = handoff or DevHandoff(parts.n)
     ho.reset()
-    sp = G.StepParams(dt, outer, starter, 1 if kill else 0, mlp)
+    mode = (G.ENCOUNTERS_KILL if kill else G.ENCOUNTERS_KEEP) if encounters is None else encounters
+    sp = G.StepParams(dt, outer, starter, mode, mlp)
     G.integrate_timeblock(parts.view, parts.n, blk.view, sp, ho.view)
     return ho.result()
 
