@@ -41,9 +41,11 @@ def _deps():
 
 
 # Translation units that must not contract a*b+c into FMA: the device
-# interpolation of the planetary history and the device track writer
-# evaluate the host restatement's formulas and are compared with it.
-PER_FILE_FLAGS = {"interp.cu": ("--fmad=false",), "track.cu": ("--fmad=false",)}
+# interpolation of the planetary history, the device track writer and the
+# device planet integrator evaluate the host restatement's formulas in its
+# operation order and are compared with it.
+PER_FILE_FLAGS = {"interp.cu": ("--fmad=false",), "track.cu": ("--fmad=false",),
+                  "planets_dev.cu": ("--fmad=false",)}
 
 
 def _compile(src, extra_flags=()):
