@@ -569,6 +569,60 @@ def check_accuracy(G, m, pr, pv, r, v, dt, n=4096, steps=1024):
             "oracle": "restatement of the reference kernel MVSKernel::step_forward (src/wh.cu:43-177)"}
 
 
+def run_reference_kernel(G, blk, r, v, dt, outer, launches=2, warmup=1):
+    """The reference's time block as the reference runs it on a GPU
+    (glisser_mvs_baseline_block: src/wh.cu:43-177 arithmetic, 24-byte vector
+    arrays, planet logs read from global memory, one particle per thread) on
+    the same workload and the same planet block, timed with CUDA events.
+    Each launch advances every particle one time block."""
+    import torch
+    dev = torch.device("cuda")
+    n = len(r)
+    tr = torch.tensor(r, dtype=torch.float64, device=dev).contiguous()
+    tv = torch.tensor(v, dtype=torch.float64, device=dev).contiguous()
+    ta = torch.zeros((n, 3), dtype=torch.float64, device=dev)
+    tf = torch.zeros(n, dtype=torch.int16, device=dev)
+    td = torch.zeros(n, dtype=torch.int32, device=dev)
+    L = int(blk["log_len"])
+    h0 = torch.tensor(np.ascontiguousarray(blk["h0_log"]), dtype=torch.float64, device=dev)
+    rl = torch.tensor(np.ascontiguousarray(blk["r_log"]), dtype=torch.float64, device=dev)
+    m = torch.tensor(blk["m"], dtype=torch.float64, device=dev)
+    ids = torch.tensor(np.asarray(blk["id"], np.uint32).view(np.int32), dtype=torch.int32, device=dev)
+    rh = torch.tensor(blk["rh"], dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream()
+    mu = float(blk["m"][0])
+
+    def launch():
+        rc = G.lib().glisser_mvs_baseline_block(tr.data_ptr(), tv.data_ptr(), ta.data_ptr(), tf.data_ptr(),
+                                                td.data_ptr(), n, L, len(blk["m"]), h0.data_ptr(), rl.data_ptr(),
+                                                m.data_ptr(), ids.data_ptr(), rh.data_ptr(), outer, dt, mu,
+                                                stream.cuda_stream)
+        if rc:
+            raise RuntimeError("glisser_mvs_baseline_block failed: %d" % rc)
+
+    for _ in range(warmup):
+        launch()
+    torch.cuda.synchronize()
+    ms, ps = 0.0, 0
+    for _ in range(launches):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        launch()
+        e1.record(stream)
+        e1.synchronize()
+        ms += e0.elapsed_time(e1)
+        ps += int(td.to(torch.int64).sum().item())
+    flagged = int((tf != 0).sum().item())
+    return {"value": ps / (ms * 1e-3), "unit": UNIT, "ms_per_launch": ms / launches, "launches": launches,
+            "particles": n, "time_block": L, "flagged_after": flagged,
+            "kernel": "mvs_baseline_kernel (glisser_mvs_baseline_block)",
+            "what": "the reference's MVSKernel::step_forward arithmetic (src/wh.cu:43-177: elliptic drift, five "
+                    "fixed Newton passes with sin/cos) in its GPU layout (24-byte vector arrays, planet logs "
+                    "from global memory, one particle per thread, 256-thread CTAs as thrust::for_each), "
+                    "compiled for sm_103a; same particles and planet block as the timed run"}
+
+
 def run_track(G, sim):
     """Track snapshot of the current state (alive particles by id, FP64
     elements, float32 records): device writer vs the host writer, wall time
@@ -640,6 +694,7 @@ def main():
     ap.add_argument("--learned-blocks", type=int, default=3)
     ap.add_argument("--no-history", action="store_true")
     ap.add_argument("--no-track", action="store_true")
+    ap.add_argument("--no-reference-kernel", action="store_true")
     ap.add_argument("--history-particles", type=int, default=2_000_000)
     ap.add_argument("--history-blocks", type=int, default=20)
     args = ap.parse_args()
@@ -765,6 +820,11 @@ def main():
                "sample": "%d particles x %d steps (%.1f s), oracle restatement of MVSKernel::step_forward "
                          "(src/wh.cu:113-177) on %d host threads" % (n_s, args.sample_steps, el, threads)}
 
+    ref_kernel = None
+    if rank == 0 and not args.no_reference_kernel:
+        ref_kernel = run_reference_kernel(G, blk0, r, v, dt, 300.0)
+        ref_kernel["timeblock_kernel_value"] = sum(psteps) / (sum(kernel_ms) * 1e-3)
+        ref_kernel["speedup"] = ref_kernel["timeblock_kernel_value"] / ref_kernel["value"]
     track = None
     if rank == 0 and not args.no_track:
         track = run_track(G, sim)
@@ -811,6 +871,7 @@ def main():
             "learned": learned,
             "history": history,
             "track": track,
+            "reference_kernel_gpu": ref_kernel,
             "accuracy": accuracy,
         }
         print(json.dumps(line), flush=True)

@@ -169,6 +169,8 @@ def lib():
             "glisser_kepler_drift_states": ([C.POINTER(ParticlesDev), C.c_size_t, C.c_double, C.c_double, C.c_int,
                                              P, P, P, P], C.c_int),
             "glisser_write_stat": ([P, C.c_char_p], C.c_int),
+            "glisser_mvs_baseline_block": ([P, P, P, P, P, C.c_size_t, C.c_uint32, C.c_uint32, P, P, P, P, P,
+                                            C.c_double, C.c_double, C.c_double, P], C.c_int),
             "glisser_swift_write_param": ([C.c_char_p, C.c_double, C.c_size_t, C.c_size_t, C.c_double, C.c_double],
                                           C.c_int),
             "glisser_swift_write_tp": ([C.c_char_p, C.c_size_t, D, D, C.c_uint32], C.c_int),
