@@ -58,18 +58,48 @@ __device__ __forceinline__ double rcp_fast(double x)
     return fma(y, fma(e, e, e), y);
 }
 
-// rsqrt to ~46 bits: one Newton step y' = y (3 - x y^2) / 2 from the seed
-// (4 FP64 ops; error <= 1.5 e^2 ~ 1e-13 relative, one-sided).  For terms
-// that are themselves small perturbations (a planet's pull next to the
-// Sun's), where 1e-13 of the term is below double rounding of the sum.
-__device__ __forceinline__ double rsqrt_fast46(double x)
+// m x^(-3/2) from m15 = 1.5 m, for a planet's pull m dr / |dr|^3 (x = |dr|^2):
+// with the FP32 seed y of x^(-1/2) and e = 1 - x y^2,
+//   m x^(-3/2) = m y^3 (1 - e)^(-3/2) ~ m y^3 (1 + 1.5 e) = m15 y^3 (5/3 - x y^2).
+// y has a float's 24-bit significand, so y^2 is exact in FP64 and the only
+// rounding in 5/3 - x y^2 is the fma's; the dropped terms, 15/8 e^2 with
+// |e| < 5e-7 from the seed, stay below 5e-13 of the pull.  5 FP64 ops (the
+// full-precision rsqrt and two cubes took 7).  For the planet terms, which
+// are themselves small perturbations next to the Sun's pull.
+__device__ __forceinline__ double pull_factor(double x, double m15)
 {
     int hi = __double2hiint(x);
-    if (!float_range(hi) || hi < 0) return rsqrt(x);
+    if (!float_range(hi) || hi < 0) {
+        double y = rsqrt(x);
+        return (m15 * (1.0 / 1.5)) * (y * y * y);
+    }
     double y = widen_bits(rsqrtf(seed_float(hi)));
-    double h = x * y;
-    double e = fma(-h, y, 1.0);
-    return fma(0.5 * y, e, y);
+    double y2 = y * y;
+    double q = fma(-x, y2, 5.0 / 3.0);
+    return ((m15 * y2) * y) * q;
+}
+
+// The float with the value of d rounded toward zero (23-bit significand),
+// built on the integer pipe (a double-to-float conversion issues to the FP64
+// pipe): +-0 when |d| < 2^-126, +-inf when |d| >= 2^128.
+__device__ __forceinline__ float f32_trunc(double d)
+{
+    int hi = __double2hiint(d);
+    unsigned lo = (unsigned)__double2loint(d);
+    int sign = hi & (int)0x80000000;
+    int e = ((hi >> 20) & 0x7FF) - (1023 - 127);
+    int bits = sign | (e << 23) | ((hi & 0xFFFFF) << 3) | (int)(lo >> 29);
+    bits = e > 0 ? bits : sign;
+    bits = e < 255 ? bits : (sign | 0x7F800000);
+    return __int_as_float(bits);
+}
+
+// The double with the value of f for finite f, on the integer pipe; +-0
+// for zero or subnormal f.
+__device__ __forceinline__ double f64_of_f32(float f)
+{
+    int b = __float_as_int(f);
+    return (b & 0x7F800000) ? widen_bits(f) : __hiloint2double(b & (int)0x80000000, 0);
 }
 
 // a < b for a >= +0 (or NaN) and finite b >= +0, on the integer pipe: the

@@ -232,7 +232,7 @@ __device__ __forceinline__ double starter_series(double dt, double rinv, double 
     double A = alpha * T2;                        // Z = -A X / 12, W = -A Y / 20, V = A^2 X / 360
     double Z = (-1.0 / 12.0) * A * X;
     double low = fma(X, fma(X, fma(-5.0, X, 2.0), -1.0), fma(Y, fma(5.0, X, -1.0), -Z));
-    float x = __double2float_rn(X), y = __double2float_rn(Y), a = __double2float_rn(A);
+    float x = f32_trunc(X), y = f32_trunc(Y), a = f32_trunc(A);
     float z = (-1.0f / 12.0f) * a * x;
     float w = (-1.0f / 20.0f) * a * y;
     float v = (1.0f / 360.0f) * a * a * x;
@@ -260,7 +260,7 @@ __device__ __forceinline__ double starter_series(double dt, double rinv, double 
     float r2c = fmaf(fmaf(-91.0f / 60.0f, x2, 39.0f / 35.0f * y), x2, -403.0f / 4200.0f * y2);
     float r3c = fmaf(4.0f / 945.0f, x2, -23.0f / 75600.0f * y);
     float o10 = 11.0f * x * fmaf(a, fmaf(a, fmaf(a, r3c, r2c), r1c), r0c);
-    return fma(T, low + (double)(((o5 + o6) + (o7 + o8)) + (o9 + o10)), T);
+    return fma(T, low + f64_of_f32(((o5 + o6) + (o7 + o8)) + (o9 + o10)), T);
 }
 
 struct DriftResult {
@@ -342,7 +342,7 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
     double mu_r = mu * rinv;
     double alpha = fma(2.0, mu_r, -v2);
     DriftResult res;
-    res.flags = alpha <= 0 ? 0x08 : 0;
+    res.flags = __double_as_longlong(alpha) <= 0 ? 0x08 : 0;   // alpha <= 0 (or negative NaN), integer pipe
     res.evals = 0;
 
     const double k = fma(-alpha, r0, mu);

@@ -100,7 +100,7 @@ __device__ __forceinline__ void issue_chunk(const Common& p, const double* log, 
 // Acceleration from planet j and its encounter test (src/wh.cu:145-160):
 // the first planet inside its radius wins (flags == 0 guard).
 __device__ __forceinline__ void planet_kick(const double* L, int j, double rx, double ry, double rz, double& ax,
-                                            double& ay, double& az, uint16_t& flags, const double* s_m,
+                                            double& ay, double& az, uint16_t& flags, const double* s_m15,
                                             const double* s_rh2, const uint32_t* s_id)
 {
     double dx = rx - L[3 * j];
@@ -108,8 +108,7 @@ __device__ __forceinline__ void planet_kick(const double* L, int j, double rx, d
     double dz = rz - L[3 * j + 2];
     double rad = fma(dx, dx, fma(dy, dy, dz * dz));
     if (lt_nonneg(rad, s_rh2[j]) && flags == 0) flags = (uint16_t)((s_id[j] << 8) | 0x0001);
-    double inv = rsqrt_fast46(rad);
-    double fac = s_m[j] * (inv * inv * inv);
+    double fac = pull_factor(rad, s_m15[j]);
     ax = fma(-dx, fac, ax);
     ay = fma(-dy, fac, ay);
     az = fma(-dz, fac, az);
@@ -118,6 +117,7 @@ __device__ __forceinline__ void planet_kick(const double* L, int j, double rx, d
 // Shared-memory state of one CTA.
 struct CtaShared {
     double m[MAX_PLANETS];
+    double m15[MAX_PLANETS];    // 1.5 m, the form the planet kick takes
     double rh2[MAX_PLANETS];
     uint32_t id[MAX_PLANETS];
     uint64_t bar[2];
@@ -215,10 +215,10 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
                 if constexpr (NP > 0) {
 #pragma unroll
                     for (int j = 1; j <= NP; j++)
-                        planet_kick(L, j, rx[k], ry[k], rz[k], aax, aay, aaz, fl, sh.m, sh.rh2, sh.id);
+                        planet_kick(L, j, rx[k], ry[k], rz[k], aax, aay, aaz, fl, sh.m15, sh.rh2, sh.id);
                 } else {
                     for (int j = 1; j <= np; j++)
-                        planet_kick(L, j, rx[k], ry[k], rz[k], aax, aay, aaz, fl, sh.m, sh.rh2, sh.id);
+                        planet_kick(L, j, rx[k], ry[k], rz[k], aax, aay, aaz, fl, sh.m15, sh.rh2, sh.id);
                 }
                 double rr = fma(rx[k], rx[k], fma(ry[k], ry[k], rz[k] * rz[k]));
                 if (lt_nonneg(rr, rh2_sun)) fl = 0x0001;
@@ -301,6 +301,7 @@ __device__ __forceinline__ void load_planet_constants(CtaShared& sh, uint32_t np
 {
     for (uint32_t j = threadIdx.x; j < npl; j += blockDim.x) {
         sh.m[j] = m[j];
+        sh.m15[j] = 1.5 * m[j];
         sh.rh2[j] = rh[j] * rh[j];
         sh.id[j] = pid[j];
     }
