@@ -58,6 +58,16 @@ __device__ __forceinline__ double rcp_fast(double x)
     return fma(y, fma(e, e, e), y);
 }
 
+// x^(-1/2) from an estimate y with relative error below ~1e-8: one Newton
+// step, y (1 + e / 2) with e = 1 - x y^2, leaves an error of 1.5 e^2 (4 FP64
+// ops; rsqrt_fast's seed needs the third-order step).
+__device__ __forceinline__ double rsqrt_refine(double x, double y)
+{
+    double h = x * y;
+    double e = fma(-h, y, 1.0);
+    return fma(0.5 * y, e, y);
+}
+
 // m x^(-3/2) from m15 = 1.5 m, for a planet's pull m dr / |dr|^3 (x = |dr|^2):
 // with the FP32 seed y of x^(-1/2) and e = 1 - x y^2,
 //   m x^(-3/2) = m y^3 (1 - e)^(-3/2) ~ m y^3 (1 + 1.5 e) = m15 y^3 (5/3 - x y^2).

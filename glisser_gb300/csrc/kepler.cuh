@@ -75,13 +75,28 @@ __device__ __forceinline__ void stumpff_short(double x, double& c2, double& c3)
     c3 = fma(x, fma(x, fma(x, -1.0 / 362880.0, 1.0 / 5040.0), -1.0 / 120.0), 1.0 / 6.0);
 }
 
+// c2, c3 to x^2 only: enough when |x| < 1e-4 (the x^3 terms, at most
+// 2.5e-17 in c2 and 2.8e-18 in c3, are below half an ulp of either)
+__device__ __forceinline__ void stumpff_tiny(double x, double& c2, double& c3)
+{
+    c2 = fma(x, fma(x, 1.0 / 720.0, -1.0 / 24.0), 0.5);
+    c3 = fma(x, fma(x, 1.0 / 5040.0, -1.0 / 120.0), 1.0 / 6.0);
+}
+
 __device__ __forceinline__ GFun gfuns(double s, double alpha)
 {
     double s2 = s * s;
     double x = alpha * s2;
     double c0, c1, c2, c3;
-    bool small = lt_nonneg(fabs(x), 2e-3);
-    if (__all_sync(__activemask(), small)) {
+    const double ax = fabs(x);
+    const unsigned lanes = __activemask();
+    if (__all_sync(lanes, lt_nonneg(ax, 1e-4))) {
+        // warp-uniform: every lane in this pass has a tiny argument (steps of
+        // a few thousandths of an orbit)
+        stumpff_tiny(x, c2, c3);
+        c1 = fma(-x, c3, 1.0);
+        c0 = fma(-x, c2, 1.0);
+    } else if (__all_sync(lanes, lt_nonneg(ax, 2e-3))) {
         // warp-uniform: every lane in this pass has a small argument
         stumpff_short(x, c2, c3);
         c1 = fma(-x, c3, 1.0);
@@ -221,11 +236,19 @@ __device__ __forceinline__ double starter_series3(double dt, double rinv, double
 // first Stumpff evaluation; orders 8-10 keep that true for eccentric orbits
 // near pericentre (tau^2 up to SERIES_TAU2_MAX).  Orders 2-4 are summed in
 // FP64, orders 5-10 (below 1e-9 of s) in FP32.
-constexpr double SERIES_TAU2_MAX = 0.01;
+constexpr float SERIES_TAU2_MAX = 0.01f;
 
-__device__ __forceinline__ double starter_series(double dt, double rinv, double alpha, double u, double k)
+// tau^2 = (dt / r0)^2 (mu / r0), the step over the local dynamical time
+// squared, in FP32 on the integer and FP32 pipes: it only chooses the
+// starter and feeds the learned starter's features.
+__device__ __forceinline__ float tau2_f32(double T, double mu_r)
 {
-    double T = dt * rinv;
+    const float t = f32_trunc(T);
+    return t * t * f32_trunc(mu_r);
+}
+
+__device__ __forceinline__ double starter_series(double T, double rinv, double alpha, double u, double k)
+{
     double T2 = T * T;
     double X = 0.5 * (u * rinv) * T;
     double Y = (k * rinv) * T2 * (1.0 / 6.0);
@@ -323,8 +346,13 @@ __device__ __forceinline__ bool kepler_laguerre(double& s, double dt, double r0,
     return false;
 }
 
-// Drifts (r, v) by dt about a central mass mu.  dt2mu = dt^2 mu (a per-
-// block constant: the step-size test compares tau^2 = dt^2 mu / r0^3);
+// Drifts (r, v) by dt about a central mass mu.  r2 = |r|^2 of the state;
+// rinv comes in as an estimate of 1/|r| (good to 1e-8 or better: the
+// previous drift's 1/f'(s), whose own error is ~1e-15) that one Newton step
+// makes exact, and goes out as the estimate for the new position.  |r| is
+// always taken from the state vector: an r0 carried from f'(s) would drift
+// away from the vector's length by rounding, and near pericentre of an
+// eccentric orbit the energy alpha = 2 mu / r0 - v^2 magnifies that.
 // tol_dt = the residual tolerance times dt (KEP_TOL * dt by default).
 // LEARNED selects the MLP starter (weights `mlp`), with the classic starter
 // outside the network's training box and as the restart when the Newton
@@ -332,13 +360,13 @@ __device__ __forceinline__ bool kepler_laguerre(double& s, double dt, double r0,
 // the classic or the series starter.
 template <bool LEARNED>
 __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, double& rz, double& vx, double& vy, double& vz,
-                                                   double r2, double dt, double mu, double dt2mu, int starter,
+                                                   double r2, double& rinv_io, double dt, double mu, int starter,
                                                    const MlpDev* mlp, double tol_dt)
 {
+    const double rinv = rsqrt_refine(r2, rinv_io);
+    const double r0 = r2 * rinv;
     double v2 = fma(vx, vx, fma(vy, vy, vz * vz));
     double u = fma(rx, vx, fma(ry, vy, rz * vz));
-    double rinv = rsqrt_fast(r2);
-    double r0 = r2 * rinv;
     double mu_r = mu * rinv;
     double alpha = fma(2.0, mu_r, -v2);
     DriftResult res;
@@ -346,17 +374,18 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
     res.evals = 0;
 
     const double k = fma(-alpha, r0, mu);
-    const double tau2 = dt2mu * (rinv * rinv) * rinv;     // (dt / dynamical time)^2
+    const double T = dt * rinv;
+    const float tau2 = tau2_f32(T, mu_r);                 // (dt / dynamical time)^2
     double s;
     [[maybe_unused]] bool from_mlp = false;
     if constexpr (LEARNED) {
-        s = starter_learned(mlp, dt, rinv, tau2, u, mu_r, alpha);
+        s = starter_learned(mlp, T, rinv, tau2, u, mu_r, alpha);
         from_mlp = s > 0;
         if (!from_mlp) s = starter_classic(dt, r0, rinv, mu, alpha, u);
     } else if (starter == STARTER_CLASSIC) {
         s = starter_classic(dt, r0, rinv, mu, alpha, u);
     } else {
-        if (lt_nonneg(tau2, SERIES_TAU2_MAX)) s = starter_series(dt, rinv, alpha, u, k);
+        if (tau2 < SERIES_TAU2_MAX) s = starter_series(T, rinv, alpha, u, k);
         else if (alpha > 0) s = starter_fp32_kepler(dt, r0, mu, alpha, u);
         else s = starter_classic(dt, r0, rinv, mu, alpha, u);
     }
@@ -378,7 +407,7 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
     }
     // fold the last correction into the G-functions (dG3 = G2 ds, dG2 =
     // G1 ds, dG1 = G0 ds; |ds| < 1e-13 s, so the second-order terms are
-    // below 1e-26)
+    // below 1e-26), and into 1/f', the inverse of the new distance
     double g3 = fma(ds, g.g2, g.g3);
     double g2 = fma(ds, g.g1, g.g2);
     double g1 = fma(ds, g.g0, g.g1);
@@ -392,6 +421,9 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
     double nvx = fma(fd, rx, gd * vx), nvy = fma(fd, ry, gd * vy), nvz = fma(fd, rz, gd * vz);
     rx = nrx; ry = nry; rz = nrz;
     vx = nvx; vy = nvy; vz = nvz;
+    // the next drift's estimate of 1/|r| (without a solution, a fresh one
+    // for whatever state the step left)
+    rinv_io = ok ? rnew_inv : rsqrt_fast(fma(rx, rx, fma(ry, ry, rz * rz)));
     return res;
 }
 

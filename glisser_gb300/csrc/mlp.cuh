@@ -23,6 +23,7 @@
 #include <cstdint>
 
 #include "../../include/glisser.h"
+#include "fastmath.cuh"
 
 namespace glisser {
 
@@ -94,18 +95,21 @@ __device__ __forceinline__ float mlp_forward(const MlpDev* __restrict__ w, float
 }
 
 // Raw features of one drift, computed in FP32 from the FP64 invariants
-// (tau2 = dt^2 mu / r0^3, mu_r = mu / r0).
-__device__ __forceinline__ void mlp_features(double tau2, double u, double rinv, double mu_r, double alpha, float& f0,
+// (tau2 = dt^2 mu / r0^3, already FP32; mu_r = mu / r0).  The doubles become
+// floats on the integer pipe (truncated, 2^-23 relative), leaving the FP64
+// pipe to the drift.
+__device__ __forceinline__ void mlp_features(float tau2, double u, double rinv, double mu_r, double alpha, float& f0,
                                              float& f1, float& f2)
 {
-    const float mr = (float)mu_r;
-    f0 = 0.5f * __logf((float)tau2);
-    f1 = (float)(u * rinv) * rsqrtf(mr);
-    f2 = __fdividef((float)alpha, mr);
+    const float mr = f32_trunc(mu_r);
+    f0 = 0.5f * __logf(tau2);
+    f1 = (f32_trunc(u) * f32_trunc(rinv)) * rsqrtf(mr);
+    f2 = __fdividef(f32_trunc(alpha), mr);
 }
 
-// Learned guess for s, or -1 when the drift is outside the training box.
-__device__ __forceinline__ double starter_learned(const MlpDev* __restrict__ w, double dt, double rinv, double tau2,
+// Learned guess for s, or -1 when the drift is outside the training box
+// (T = dt / r0, tau2 = T^2 mu / r0 in FP32).
+__device__ __forceinline__ double starter_learned(const MlpDev* __restrict__ w, double T, double rinv, float tau2,
                                                   double u, double mu_r, double alpha)
 {
     float f0, f1, f2;
@@ -118,7 +122,7 @@ __device__ __forceinline__ double starter_learned(const MlpDev* __restrict__ w, 
     const float x1 = (f1 - n.in_mean[1]) * n.in_scale[1];
     const float x2 = (f2 - n.in_mean[2]) * n.in_scale[2];
     const float z = fmaf(n.out_scale, mlp_forward(w, x0, x1, x2), n.out_mean);
-    return (dt * rinv) * (double)__expf(z * sqrtf((float)tau2));
+    return T * f64_of_f32(__expf(z * sqrtf(tau2)));
 }
 
 }  // namespace glisser

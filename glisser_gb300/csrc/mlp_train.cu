@@ -79,7 +79,7 @@ __global__ void log_solves_kernel(glisser_particles pa, uint32_t n, double dt, d
         if (!ok) ok = kepler_laguerre(s, dt, r0, u, mu, alpha, k, tol, g, fpp, inv_fp, ds, ev);
         evals = ev;
         float f0, f1, f2;
-        mlp_features(tau2, u, rinv, mu_r, alpha, f0, f1, f2);
+        mlp_features(tau2_f32(dt * rinv, mu_r), u, rinv, mu_r, alpha, f0, f1, f2);
         const double sf = s + ds;
         feat[3 * (size_t)i] = f0;
         feat[3 * (size_t)i + 1] = f1;
@@ -311,7 +311,8 @@ __global__ void drift_states_kernel(glisser_particles pa, uint32_t n, double dt,
     if (i >= n) return;
     double rx = pa.rx[i], ry = pa.ry[i], rz = pa.rz[i], vx = pa.vx[i], vy = pa.vy[i], vz = pa.vz[i];
     const double r2 = fma(rx, rx, fma(ry, ry, rz * rz));
-    DriftResult d = kepler_drift<LEARNED>(rx, ry, rz, vx, vy, vz, r2, dt, mu, dt * dt * mu, starter, mlp, KEP_TOL * dt);
+    double rinv = rsqrt_fast(r2);
+    DriftResult d = kepler_drift<LEARNED>(rx, ry, rz, vx, vy, vz, r2, rinv, dt, mu, starter, mlp, KEP_TOL * dt);
     pa.rx[i] = rx; pa.ry[i] = ry; pa.rz[i] = rz;
     pa.vx[i] = vx; pa.vy[i] = vy; pa.vz[i] = vz;
     if (evals) evals[i] = d.evals;

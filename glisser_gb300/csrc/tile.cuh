@@ -145,13 +145,12 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
         if (nchunks > 1) { issue_chunk(p, log, stage + bufstride, &sh.bar[1], 1, rec); inflight1 = true; }
     }
 
-    double rx[PPT], ry[PPT], rz[PPT], vx[PPT], vy[PPT], vz[PPT], ax[PPT], ay[PPT], az[PPT], r2[PPT];
+    double rx[PPT], ry[PPT], rz[PPT], vx[PPT], vy[PPT], vz[PPT], ax[PPT], ay[PPT], az[PPT], r2[PPT], rinv[PPT];
     uint16_t flags[PPT], flags0[PPT];
     uint32_t dti[PPT];
     uint32_t evals = 0;
     const double hdt = p.dt * 0.5;
     const double mu = sh.m[0];
-    const double dt2mu = p.dt * p.dt * mu;
     const double rh2_sun = sh.rh2[0];
 #pragma unroll
     for (int k = 0; k < PPT; k++) {
@@ -171,13 +170,15 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
         // merged into one full kick (v += a dt); a particle takes the closing
         // half kick when it is flagged or the block ends, so its stored
         // velocity is always at a step boundary.  |r|^2 from the Sun/outer
-        // test is the next drift's r0^2.
+        // test is the next drift's r0^2; each drift also hands the next one
+        // its estimate of 1/|r|.
         if (flags[k] == 0 && p.len > 0) {
             vx[k] = fma(ax[k], hdt, vx[k]);
             vy[k] = fma(ay[k], hdt, vy[k]);
             vz[k] = fma(az[k], hdt, vz[k]);
         }
         r2[k] = fma(rx[k], rx[k], fma(ry[k], ry[k], rz[k] * rz[k]));
+        rinv[k] = rsqrt_fast(r2[k]);
     }
 
     bool ok = true;
@@ -207,8 +208,8 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
 #pragma unroll
             for (int k = 0; k < PPT; k++) {
                 if (flags[k] != 0) continue;
-                DriftResult d = kepler_drift<LEARNED>(rx[k], ry[k], rz[k], vx[k], vy[k], vz[k], r2[k], p.dt, mu, dt2mu,
-                                                       p.starter, p.mlp, p.tol_dt);
+                DriftResult d = kepler_drift<LEARNED>(rx[k], ry[k], rz[k], vx[k], vy[k], vz[k], r2[k], rinv[k], p.dt,
+                                                       mu, p.starter, p.mlp, p.tol_dt);
                 uint16_t fl = d.flags;
                 evals += d.evals;
                 double aax = L[0], aay = L[1], aaz = L[2];
@@ -220,7 +221,7 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
                     for (int j = 1; j <= np; j++)
                         planet_kick(L, j, rx[k], ry[k], rz[k], aax, aay, aaz, fl, sh.m15, sh.rh2, sh.id);
                 }
-                double rr = fma(rx[k], rx[k], fma(ry[k], ry[k], rz[k] * rz[k]));
+                const double rr = fma(rx[k], rx[k], fma(ry[k], ry[k], rz[k] * rz[k]));
                 if (lt_nonneg(rr, rh2_sun)) fl = 0x0001;
                 if (gt_nonneg(rr, p.outer2)) fl = 0x0002;
                 r2[k] = rr;
