@@ -10,9 +10,23 @@ namespace {
 
 using namespace tile;
 
-// Persistent kernel over (system, tile) work items.
+// Resident threads per SM the ensemble kernel's registers are sized for
+// (plain and learned starter); a build-time tuning knob.
+#ifndef GLISSER_BATCHED_THREADS_PER_SM
+#define GLISSER_BATCHED_THREADS_PER_SM 512
+#endif
+#ifndef GLISSER_BATCHED_THREADS_PER_SM_LEARNED
+#define GLISSER_BATCHED_THREADS_PER_SM_LEARNED 384
+#endif
+
+// Persistent kernel over (system, tile) work items.  Register budget: 128
+// per thread (512 resident threads per SM), or 168 for the learned starter,
+// whose network inference holds 32 hidden activations (384 threads); left
+// free, the compiler sized some learned instantiations for higher occupancy
+// and spilled inside the step loop.
 template <int NP, int CTA, int PPT, bool LEARNED>
-__global__ void __launch_bounds__(CTA)
+__global__ void __launch_bounds__(CTA, (LEARNED ? GLISSER_BATCHED_THREADS_PER_SM_LEARNED
+                                                : GLISSER_BATCHED_THREADS_PER_SM) / CTA)
     batched_kernel(const Common p, BatchSystems sys, const BatchItem* items, const uint32_t* n_items, uint32_t* queue)
 {
     extern __shared__ __align__(128) double stage[];

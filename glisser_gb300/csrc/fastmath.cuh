@@ -58,14 +58,13 @@ __device__ __forceinline__ double rcp_fast(double x)
     return fma(y, fma(e, e, e), y);
 }
 
-// x^(-1/2) from an estimate y with relative error below ~1e-8: one Newton
-// step, y (1 + e / 2) with e = 1 - x y^2, leaves an error of 1.5 e^2 (4 FP64
-// ops; rsqrt_fast's seed needs the third-order step).
-__device__ __forceinline__ double rsqrt_refine(double x, double y)
+// 1/x to FP32 accuracy (~2^-22 relative) with no FP64 instruction, for
+// corrections that are themselves tiny.
+__device__ __forceinline__ double rcp_seed(double x)
 {
-    double h = x * y;
-    double e = fma(-h, y, 1.0);
-    return fma(0.5 * y, e, y);
+    int hi = __double2hiint(x);
+    if (!float_range(hi)) return 1.0 / x;
+    return widen_bits(__frcp_rn(seed_float(hi)));
 }
 
 // m x^(-3/2) from m15 = 1.5 m, for a planet's pull m dr / |dr|^3 (x = |dr|^2):

@@ -247,11 +247,11 @@ __device__ __forceinline__ float tau2_f32(double T, double mu_r)
     return t * t * f32_trunc(mu_r);
 }
 
-__device__ __forceinline__ double starter_series(double T, double rinv, double alpha, double u, double k)
+__device__ __forceinline__ double starter_series(double T, double rinv, double alpha, double u, double kr)
 {
     double T2 = T * T;
     double X = 0.5 * (u * rinv) * T;
-    double Y = (k * rinv) * T2 * (1.0 / 6.0);
+    double Y = kr * T2 * (1.0 / 6.0);
     double A = alpha * T2;                        // Z = -A X / 12, W = -A Y / 20, V = A^2 X / 360
     double Z = (-1.0 / 12.0) * A * X;
     double low = fma(X, fma(X, fma(-5.0, X, 2.0), -1.0), fma(Y, fma(5.0, X, -1.0), -Z));
@@ -292,25 +292,27 @@ struct DriftResult {
 };
 
 // Quartic Newton passes from s (at most KEP_NEWTON_MAX).  On acceptance
-// (|f| < tol at the current s) returns true with the G-functions at s, f''
-// and 1/f' there and the pending Newton correction ds = -f/f'.
+// (|f| < tol at the current s) returns true with the G-functions at s and
+// the pending Newton correction ds = -f/f'.  |ds| < tol s there, so ds needs
+// only a few correct digits: it takes the FP32 reciprocal of f', and f'' is
+// formed only for the passes that go on.
 __device__ __forceinline__ bool kepler_newton(double& s, double dt, double r0, double u, double mu, double alpha,
-                                              double k, double tol, GFun& g, double& fpp, double& inv_fp, double& ds,
-                                              uint16_t& evals)
+                                              double tol, GFun& g, double& ds, uint16_t& evals)
 {
     for (int it = 0; it < KEP_NEWTON_MAX; it++) {
         g = gfuns(s, alpha);
         evals++;
         double f = fma(r0, g.g1, fma(u, g.g2, fma(mu, g.g3, -dt)));
         double fp = fma(r0, g.g0, fma(u, g.g1, mu * g.g2));
-        fpp = fma(k, g.g1, u * g.g0);
-        inv_fp = rcp_fast(fp);
-        double h = f * inv_fp;
         if (lt_nonneg(fabs(f), tol)) {
             // accepted: a Newton correction is exact to O(h^2) ~ 1e-26
-            ds = -h;
+            ds = -f * rcp_seed(fp);
             return true;
         }
+        const double k = fma(-alpha, r0, mu);
+        double fpp = fma(k, g.g1, u * g.g0);
+        double inv_fp = rcp_fast(fp);
+        double h = f * inv_fp;
         double fppp = fma(k, g.g0, -(u * alpha) * g.g1);
         double q = fpp * inv_fp;                      // 2A
         double p = fppp * inv_fp;                     // 6B
@@ -325,19 +327,18 @@ __device__ __forceinline__ bool kepler_newton(double& s, double dt, double r0, d
 // f'' = (mu - alpha r0) G1 + u G0), at most KEP_LAGUERRE_MAX passes; same
 // outputs as kepler_newton.
 __device__ __forceinline__ bool kepler_laguerre(double& s, double dt, double r0, double u, double mu, double alpha,
-                                             double k, double tol, GFun& g, double& fpp, double& inv_fp, double& ds,
-                                             uint16_t& evals)
+                                             double tol, GFun& g, double& ds, uint16_t& evals)
 {
     const double ln = 5.0;
+    const double k = fma(-alpha, r0, mu);
     for (int it = 0; it < KEP_LAGUERRE_MAX; it++) {
         g = gfuns(s, alpha);
         evals++;
         double f = fma(r0, g.g1, fma(u, g.g2, fma(mu, g.g3, -dt)));
         double fp = fma(r0, g.g0, fma(u, g.g1, mu * g.g2));
-        fpp = fma(k, g.g1, u * g.g0);
-        inv_fp = 1.0 / fp;
+        double fpp = fma(k, g.g1, u * g.g0);
         if (fabs(f) < tol) {
-            ds = -f * inv_fp;
+            ds = -f / fp;
             return true;
         }
         double disc = sqrt(fabs((ln - 1.0) * (ln - 1.0) * fp * fp - (ln - 1.0) * ln * f * fpp));
@@ -346,25 +347,23 @@ __device__ __forceinline__ bool kepler_laguerre(double& s, double dt, double r0,
     return false;
 }
 
-// Drifts (r, v) by dt about a central mass mu.  r2 = |r|^2 of the state;
-// rinv comes in as an estimate of 1/|r| (good to 1e-8 or better: the
-// previous drift's 1/f'(s), whose own error is ~1e-15) that one Newton step
-// makes exact, and goes out as the estimate for the new position.  |r| is
-// always taken from the state vector: an r0 carried from f'(s) would drift
-// away from the vector's length by rounding, and near pericentre of an
-// eccentric orbit the energy alpha = 2 mu / r0 - v^2 magnifies that.
-// tol_dt = the residual tolerance times dt (KEP_TOL * dt by default).
-// LEARNED selects the MLP starter (weights `mlp`), with the classic starter
-// outside the network's training box and as the restart when the Newton
-// passes from the learned guess do not converge; otherwise `starter` picks
-// the classic or the series starter.
+// Drifts (r, v) by dt about a central mass mu.  r2 = |r|^2 and rinv = 1/|r|
+// come in for the state and go out for the new position, both taken from the
+// new position vector itself (its length enters the energy alpha = 2 mu / r0
+// - v^2 of the next drift, where near pericentre of an eccentric orbit any
+// inconsistency with the vector is magnified).  tol_dt = the residual
+// tolerance times dt (KEP_TOL * dt by default).  LEARNED selects the MLP
+// starter (weights `mlp`), with the classic starter outside the network's
+// training box and as the restart when the Newton passes from the learned
+// guess do not converge; otherwise `starter` picks the classic or the series
+// starter.
 template <bool LEARNED>
 __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, double& rz, double& vx, double& vy, double& vz,
-                                                   double r2, double& rinv_io, double dt, double mu, int starter,
+                                                   double& r2_io, double& rinv_io, double dt, double mu, int starter,
                                                    const MlpDev* mlp, double tol_dt)
 {
-    const double rinv = rsqrt_refine(r2, rinv_io);
-    const double r0 = r2 * rinv;
+    const double rinv = rinv_io;
+    const double r0 = r2_io * rinv;
     double v2 = fma(vx, vx, fma(vy, vy, vz * vz));
     double u = fma(rx, vx, fma(ry, vy, rz * vz));
     double mu_r = mu * rinv;
@@ -373,7 +372,6 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
     res.flags = __double_as_longlong(alpha) <= 0 ? 0x08 : 0;   // alpha <= 0 (or negative NaN), integer pipe
     res.evals = 0;
 
-    const double k = fma(-alpha, r0, mu);
     const double T = dt * rinv;
     const float tau2 = tau2_f32(T, mu_r);                 // (dt / dynamical time)^2
     double s;
@@ -385,45 +383,46 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
     } else if (starter == STARTER_CLASSIC) {
         s = starter_classic(dt, r0, rinv, mu, alpha, u);
     } else {
-        if (tau2 < SERIES_TAU2_MAX) s = starter_series(T, rinv, alpha, u, k);
+        // (mu - alpha r0) / r0 = mu / r0 - alpha
+        if (tau2 < SERIES_TAU2_MAX) s = starter_series(T, rinv, alpha, u, mu_r - alpha);
         else if (alpha > 0) s = starter_fp32_kepler(dt, r0, mu, alpha, u);
         else s = starter_classic(dt, r0, rinv, mu, alpha, u);
     }
 
     const double tol = tol_dt;
     GFun g;
-    double fpp = 0, ds = 0, inv_fp = 0;
-    bool ok = kepler_newton(s, dt, r0, u, mu, alpha, k, tol, g, fpp, inv_fp, ds, res.evals);
+    double ds = 0;
+    bool ok = kepler_newton(s, dt, r0, u, mu, alpha, tol, g, ds, res.evals);
     if constexpr (LEARNED) {
         if (!ok && from_mlp) {
             s = starter_classic(dt, r0, rinv, mu, alpha, u);
-            ok = kepler_newton(s, dt, r0, u, mu, alpha, k, tol, g, fpp, inv_fp, ds, res.evals);
+            ok = kepler_newton(s, dt, r0, u, mu, alpha, tol, g, ds, res.evals);
         }
     }
-    if (!ok) ok = kepler_laguerre(s, dt, r0, u, mu, alpha, k, tol, g, fpp, inv_fp, ds, res.evals);
+    if (!ok) ok = kepler_laguerre(s, dt, r0, u, mu, alpha, tol, g, ds, res.evals);
     if (!ok) {
         res.flags |= 0x04;
         ds = 0;
     }
     // fold the last correction into the G-functions (dG3 = G2 ds, dG2 =
     // G1 ds, dG1 = G0 ds; |ds| < 1e-13 s, so the second-order terms are
-    // below 1e-26), and into 1/f', the inverse of the new distance
+    // below 1e-26)
     double g3 = fma(ds, g.g2, g.g3);
     double g2 = fma(ds, g.g1, g.g2);
     double g1 = fma(ds, g.g0, g.g1);
-    double rnew_inv = inv_fp * fma(-fpp * ds, inv_fp, 1.0);    // 1/f'(s+ds)
 
     double ff = fma(-mu_r, g2, 1.0);
     double gg = fma(-mu, g3, dt);
-    double fd = -mu_r * g1 * rnew_inv;
-    double gd = fma(-mu * g2, rnew_inv, 1.0);
     double nrx = fma(ff, rx, gg * vx), nry = fma(ff, ry, gg * vy), nrz = fma(ff, rz, gg * vz);
+    const double nr2 = fma(nrx, nrx, fma(nry, nry, nrz * nrz));
+    const double nrinv = rsqrt_fast(nr2);
+    double fd = -mu_r * g1 * nrinv;
+    double gd = fma(-mu * g2, nrinv, 1.0);
     double nvx = fma(fd, rx, gd * vx), nvy = fma(fd, ry, gd * vy), nvz = fma(fd, rz, gd * vz);
     rx = nrx; ry = nry; rz = nrz;
     vx = nvx; vy = nvy; vz = nvz;
-    // the next drift's estimate of 1/|r| (without a solution, a fresh one
-    // for whatever state the step left)
-    rinv_io = ok ? rnew_inv : rsqrt_fast(fma(rx, rx, fma(ry, ry, rz * rz)));
+    r2_io = nr2;
+    rinv_io = nrinv;
     return res;
 }
 

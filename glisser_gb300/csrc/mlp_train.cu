@@ -67,16 +67,15 @@ __global__ void log_solves_kernel(glisser_particles pa, uint32_t n, double dt, d
         const double r0 = r2 * rinv;
         const double mu_r = mu * rinv;
         const double alpha = fma(2.0, mu_r, -v2);
-        const double k = fma(-alpha, r0, mu);
         const double dt2mu = dt * dt * mu;
         const double tau2 = dt2mu * (rinv * rinv) * rinv;
         double s = starter_classic(dt, r0, rinv, mu, alpha, u);
         const double tol = KEP_TOL * dt;
         GFun g;
-        double fpp = 0, inv_fp = 0, ds = 0;
+        double ds = 0;
         uint16_t ev = 0;
-        bool ok = kepler_newton(s, dt, r0, u, mu, alpha, k, tol, g, fpp, inv_fp, ds, ev);
-        if (!ok) ok = kepler_laguerre(s, dt, r0, u, mu, alpha, k, tol, g, fpp, inv_fp, ds, ev);
+        bool ok = kepler_newton(s, dt, r0, u, mu, alpha, tol, g, ds, ev);
+        if (!ok) ok = kepler_laguerre(s, dt, r0, u, mu, alpha, tol, g, ds, ev);
         evals = ev;
         float f0, f1, f2;
         mlp_features(tau2_f32(dt * rinv, mu_r), u, rinv, mu_r, alpha, f0, f1, f2);
@@ -311,8 +310,8 @@ __global__ void drift_states_kernel(glisser_particles pa, uint32_t n, double dt,
     if (i >= n) return;
     double rx = pa.rx[i], ry = pa.ry[i], rz = pa.rz[i], vx = pa.vx[i], vy = pa.vy[i], vz = pa.vz[i];
     const double r2 = fma(rx, rx, fma(ry, ry, rz * rz));
-    double rinv = rsqrt_fast(r2);
-    DriftResult d = kepler_drift<LEARNED>(rx, ry, rz, vx, vy, vz, r2, rinv, dt, mu, starter, mlp, KEP_TOL * dt);
+    double r2v = r2, rinv = rsqrt_fast(r2);
+    DriftResult d = kepler_drift<LEARNED>(rx, ry, rz, vx, vy, vz, r2v, rinv, dt, mu, starter, mlp, KEP_TOL * dt);
     pa.rx[i] = rx; pa.ry[i] = ry; pa.rz[i] = rz;
     pa.vx[i] = vx; pa.vy[i] = vy; pa.vz[i] = vz;
     if (evals) evals[i] = d.evals;

@@ -169,9 +169,9 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
         // Kick-drift-kick with the two half kicks between consecutive steps
         // merged into one full kick (v += a dt); a particle takes the closing
         // half kick when it is flagged or the block ends, so its stored
-        // velocity is always at a step boundary.  |r|^2 from the Sun/outer
-        // test is the next drift's r0^2; each drift also hands the next one
-        // its estimate of 1/|r|.
+        // velocity is always at a step boundary.  Each drift returns |r|^2 and
+        // 1/|r| of the position it produces: the Sun/outer test's and the next
+        // drift's.
         if (flags[k] == 0 && p.len > 0) {
             vx[k] = fma(ax[k], hdt, vx[k]);
             vy[k] = fma(ay[k], hdt, vy[k]);
@@ -221,10 +221,9 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
                     for (int j = 1; j <= np; j++)
                         planet_kick(L, j, rx[k], ry[k], rz[k], aax, aay, aaz, fl, sh.m15, sh.rh2, sh.id);
                 }
-                const double rr = fma(rx[k], rx[k], fma(ry[k], ry[k], rz[k] * rz[k]));
+                const double rr = r2[k];
                 if (lt_nonneg(rr, rh2_sun)) fl = 0x0001;
                 if (gt_nonneg(rr, p.outer2)) fl = 0x0002;
-                r2[k] = rr;
                 flags[k] = fl;
                 ax[k] = aax; ay[k] = aay; az[k] = aaz;
                 dti[k] = cfirst + s + 1;
