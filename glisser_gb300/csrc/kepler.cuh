@@ -87,24 +87,19 @@ __device__ __forceinline__ GFun gfuns(double s, double alpha)
 {
     double s2 = s * s;
     double x = alpha * s2;
-    double c0, c1, c2, c3;
+    double c2, c3;
+    GFun g;
     const double ax = fabs(x);
     const unsigned lanes = __activemask();
     if (__all_sync(lanes, lt_nonneg(ax, 1e-4))) {
         // warp-uniform: every lane in this pass has a tiny argument (steps of
         // a few thousandths of an orbit)
         stumpff_tiny(x, c2, c3);
-        c1 = fma(-x, c3, 1.0);
-        c0 = fma(-x, c2, 1.0);
     } else if (__all_sync(lanes, lt_nonneg(ax, 2e-3))) {
         // warp-uniform: every lane in this pass has a small argument
         stumpff_short(x, c2, c3);
-        c1 = fma(-x, c3, 1.0);
-        c0 = fma(-x, c2, 1.0);
     } else if (fabs(x) < 0.1) {
         stumpff_small(x, c2, c3);
-        c1 = fma(-x, c3, 1.0);
-        c0 = fma(-x, c2, 1.0);
     } else {
         // quarter the argument until |x| < 0.1, then rebuild (bounded: x
         // finite needs at most ~520 quarterings; non-finite x stops at 600)
@@ -114,20 +109,26 @@ __device__ __forceinline__ GFun gfuns(double s, double alpha)
             n++;
         }
         stumpff_small(x, c2, c3);
-        c1 = fma(-x, c3, 1.0);
-        c0 = fma(-x, c2, 1.0);
+        double c1 = fma(-x, c3, 1.0);
+        double c0 = fma(-x, c2, 1.0);
         for (int i = 0; i < n; i++) {
             c3 = (c2 + c0 * c3) * 0.25;
             c2 = c1 * c1 * 0.5;
             c1 = c0 * c1;
             c0 = fma(2.0 * c0, c0, -1.0);
         }
+        g.g0 = c0;
+        g.g1 = s * c1;
+        g.g2 = s2 * c2;
+        g.g3 = s2 * s * c3;
+        return g;
     }
-    GFun g;
-    g.g0 = c0;
-    g.g1 = s * c1;
+    // c1 = 1 - x c3 and c0 = 1 - x c2 folded into G1 = s - alpha G3 and
+    // G0 = 1 - alpha G2
     g.g2 = s2 * c2;
-    g.g3 = s2 * s * c3;
+    g.g3 = s * (s2 * c3);
+    g.g1 = fma(-alpha, g.g3, s);
+    g.g0 = fma(-alpha, g.g2, 1.0);
     return g;
 }
 
@@ -250,12 +251,14 @@ __device__ __forceinline__ float tau2_f32(double T, double mu_r)
 __device__ __forceinline__ double starter_series(double T, double rinv, double alpha, double u, double kr)
 {
     double T2 = T * T;
-    double X = 0.5 * (u * rinv) * T;
-    double Y = kr * T2 * (1.0 / 6.0);
+    // X2 = 2X and Y6 = 6Y carry the factors 1/2 and 1/6 into the constants
+    double X2 = (u * rinv) * T;
+    double Y6 = kr * T2;
     double A = alpha * T2;                        // Z = -A X / 12, W = -A Y / 20, V = A^2 X / 360
-    double Z = (-1.0 / 12.0) * A * X;
-    double low = fma(X, fma(X, fma(-5.0, X, 2.0), -1.0), fma(Y, fma(5.0, X, -1.0), -Z));
-    float x = f32_trunc(X), y = f32_trunc(Y), a = f32_trunc(A);
+    // X (X (2 - 5X) - 1) + Y (5X - 1) - Z
+    double low = fma(X2, fma(X2, fma(-0.625, X2, 0.5), -0.5),
+                     fma(Y6, fma(5.0 / 12.0, X2, -1.0 / 6.0), A * X2 * (1.0 / 24.0)));
+    float x = 0.5f * f32_trunc(X2), y = f32_trunc(Y6) * (1.0f / 6.0f), a = f32_trunc(A);
     float z = (-1.0f / 12.0f) * a * x;
     float w = (-1.0f / 20.0f) * a * y;
     float v = (1.0f / 360.0f) * a * a * x;
