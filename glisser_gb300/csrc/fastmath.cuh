@@ -111,6 +111,79 @@ __device__ __forceinline__ double f64_of_f32(float f)
     return (b & 0x7F800000) ? widen_bits(f) : __hiloint2double(b & (int)0x80000000, 0);
 }
 
+// ---------------------------------------------------------------------------
+// Float-float numbers: the unevaluated sum hi + lo of two floats, ~48
+// significant bits, with arithmetic on the FP32 pipe by error-free
+// transformations (Dekker's product through the FMA, Knuth's two-sum; see
+// Joldes, Muller, Popescu, "Tight and rigorous error bounds for basic
+// building blocks of double-word arithmetic", ACM TOMS 44, 2017).  The
+// __f*_rn intrinsics keep the compiler from contracting the sums and
+// products the transformations rely on.
+struct ff {
+    float hi, lo;
+};
+
+__device__ __forceinline__ ff ff_fast_two_sum(float a, float b)   // |a| >= |b| or a == 0
+{
+    const float s = __fadd_rn(a, b);
+    return { s, __fsub_rn(b, __fsub_rn(s, a)) };
+}
+
+__device__ __forceinline__ ff ff_two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return { s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb)) };
+}
+
+__device__ __forceinline__ ff ff_add(ff a, ff b)
+{
+    const ff s = ff_two_sum(a.hi, b.hi);
+    return ff_fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+
+__device__ __forceinline__ ff ff_add_f(ff a, float b)
+{
+    const ff s = ff_two_sum(a.hi, b);
+    return ff_fast_two_sum(s.hi, __fadd_rn(s.lo, a.lo));
+}
+
+__device__ __forceinline__ ff ff_mul(ff a, ff b)
+{
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    return ff_fast_two_sum(p, e);
+}
+
+__device__ __forceinline__ ff ff_mul_f(ff a, float b)
+{
+    const float p = __fmul_rn(a.hi, b);
+    float e = __fmaf_rn(a.hi, b, -p);
+    e = __fmaf_rn(a.lo, b, e);
+    return ff_fast_two_sum(p, e);
+}
+
+__device__ __forceinline__ ff ff_scale(ff a, float pow2) { return { a.hi * pow2, a.lo * pow2 }; }   // exact
+__device__ __forceinline__ ff ff_neg(ff a) { return { -a.hi, -a.lo }; }
+
+// A double as a float-float on the integer pipe: hi = d rounded toward zero
+// to 24 significant bits, lo = the remaining 29 significand bits rounded
+// toward zero to 24 (|d - hi - lo| < 2^-47 |d|).  For |d| within
+// [2^-96, 2^127); zero gives zero; smaller magnitudes lose lo.
+__device__ __forceinline__ ff ff_split(double d)
+{
+    const int hw = __double2hiint(d);
+    const unsigned rem = (unsigned)__double2loint(d) & 0x1FFFFFFFu;
+    const float h = f32_trunc(d);
+    const int top = 31 - __clz(rem);                      // -1 when rem == 0
+    const unsigned m = top >= 23 ? rem >> (top - 23) : rem << (23 - top);
+    const int fe = ((hw >> 20) & 0x7FF) - 1023 - 52 + top + 127;   // biased exponent of lo
+    const int bits = (hw & (int)0x80000000) | (fe << 23) | (int)(m & 0x7FFFFFu);
+    return { h, (rem != 0 && fe > 0) ? __int_as_float(bits) : 0.0f };
+}
+
 // a < b for a >= +0 (or NaN) and finite b >= +0, on the integer pipe: the
 // IEEE bit patterns of non-negative doubles order like the integers; a NaN a
 // of either sign compares false, as in floating point.

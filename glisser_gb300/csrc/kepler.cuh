@@ -248,17 +248,25 @@ __device__ __forceinline__ float tau2_f32(double T, double mu_r)
     return t * t * f32_trunc(mu_r);
 }
 
-__device__ __forceinline__ double starter_series(double T, double rinv, double alpha, double u, double kr)
+__device__ __forceinline__ double starter_series(double T, double rinv, double alpha, double u, double mu_r)
 {
-    double T2 = T * T;
-    // X2 = 2X and Y6 = 6Y carry the factors 1/2 and 1/6 into the constants
-    double X2 = (u * rinv) * T;
-    double Y6 = kr * T2;
-    double A = alpha * T2;                        // Z = -A X / 12, W = -A Y / 20, V = A^2 X / 360
-    // X (X (2 - 5X) - 1) + Y (5X - 1) - Z
-    double low = fma(X2, fma(X2, fma(-0.625, X2, 0.5), -0.5),
-                     fma(Y6, fma(5.0 / 12.0, X2, -1.0 / 6.0), A * X2 * (1.0 / 24.0)));
-    float x = 0.5f * f32_trunc(X2), y = f32_trunc(Y6) * (1.0f / 6.0f), a = f32_trunc(A);
+    // orders 2-4 in float-float from float-float inputs (X = u T / (2 r0),
+    // Y = (mu / r0 - alpha) T^2 / 6, A = alpha T^2): the FP32 pipe does the
+    // work, leaving two FP64 operations (the final s = T (1 + w))
+    const ff t = ff_split(T), al = ff_split(alpha);
+    const ff t2 = ff_mul(t, t);
+    const ff X = ff_scale(ff_mul(ff_mul(ff_split(u), ff_split(rinv)), t), 0.5f);
+    const ff sixth = { 1.0f / 6.0f, -4.9670538e-09f };   // 1/6 = hi + lo to 48 bits
+    const ff twelfth = { 1.0f / 12.0f, -2.4835269e-09f };
+    const ff Y = ff_mul(ff_mul(ff_add(ff_split(mu_r), ff_neg(al)), t2), sixth);
+    const ff A = ff_mul(al, t2);
+    // X (X (2 - 5X) - 1) + Y (5X - 1) - Z,  Z = -A X / 12
+    const ff p25 = ff_add_f(ff_mul_f(X, -5.0f), 2.0f);
+    const ff t1 = ff_mul(X, ff_add_f(ff_mul(X, p25), -1.0f));
+    const ff t2y = ff_mul(Y, ff_add_f(ff_mul_f(X, 5.0f), -1.0f));
+    const ff t3 = ff_mul(ff_mul(A, X), twelfth);
+    const ff low = ff_add(ff_add(t1, t2y), t3);
+    float x = X.hi, y = Y.hi, a = A.hi;
     float z = (-1.0f / 12.0f) * a * x;
     float w = (-1.0f / 20.0f) * a * y;
     float v = (1.0f / 360.0f) * a * a * x;
@@ -286,7 +294,8 @@ __device__ __forceinline__ double starter_series(double T, double rinv, double a
     float r2c = fmaf(fmaf(-91.0f / 60.0f, x2, 39.0f / 35.0f * y), x2, -403.0f / 4200.0f * y2);
     float r3c = fmaf(4.0f / 945.0f, x2, -23.0f / 75600.0f * y);
     float o10 = 11.0f * x * fmaf(a, fmaf(a, fmaf(a, r3c, r2c), r1c), r0c);
-    return fma(T, low + f64_of_f32(((o5 + o6) + (o7 + o8)) + (o9 + o10)), T);
+    const ff sum = ff_add_f(low, ((o5 + o6) + (o7 + o8)) + (o9 + o10));
+    return fma(T, f64_of_f32(sum.hi) + f64_of_f32(sum.lo), T);
 }
 
 struct DriftResult {
@@ -386,8 +395,7 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
     } else if (starter == STARTER_CLASSIC) {
         s = starter_classic(dt, r0, rinv, mu, alpha, u);
     } else {
-        // (mu - alpha r0) / r0 = mu / r0 - alpha
-        if (tau2 < SERIES_TAU2_MAX) s = starter_series(T, rinv, alpha, u, mu_r - alpha);
+        if (tau2 < SERIES_TAU2_MAX) s = starter_series(T, rinv, alpha, u, mu_r);
         else if (alpha > 0) s = starter_fp32_kepler(dt, r0, mu, alpha, u);
         else s = starter_classic(dt, r0, rinv, mu, alpha, u);
     }
