@@ -165,6 +165,22 @@ __device__ __forceinline__ ff ff_mul_f(ff a, float b)
     return ff_fast_two_sum(p, e);
 }
 
+__device__ __forceinline__ ff ff_two_prod(float a, float b)
+{
+    const float p = __fmul_rn(a, b);
+    return { p, __fmaf_rn(a, b, -p) };
+}
+
+__device__ __forceinline__ ff ff_sqr(ff a)
+{
+    const float p = __fmul_rn(a.hi, a.hi);
+    float e = __fmaf_rn(a.hi, a.hi, -p);
+    e = __fmaf_rn(__fmul_rn(2.0f, a.hi), a.lo, e);
+    return ff_fast_two_sum(p, e);
+}
+
+__device__ __forceinline__ bool ff_lt(ff a, ff b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+
 __device__ __forceinline__ ff ff_scale(ff a, float pow2) { return { a.hi * pow2, a.lo * pow2 }; }   // exact
 __device__ __forceinline__ ff ff_neg(ff a) { return { -a.hi, -a.lo }; }
 
@@ -182,6 +198,31 @@ __device__ __forceinline__ ff ff_split(double d)
     const int fe = ((hw >> 20) & 0x7FF) - 1023 - 52 + top + 127;   // biased exponent of lo
     const int bits = (hw & (int)0x80000000) | (fe << 23) | (int)(m & 0x7FFFFFu);
     return { h, (rem != 0 && fe > 0) ? __int_as_float(bits) : 0.0f };
+}
+
+// m x^(-3/2) for float-float x = |dr|^2 and m (a planet's pull, as
+// pull_factor), on the FP32 pipe: the seed y = rsqrtf(x.hi), e = 1 - x y^2
+// with x y^2 in float-float (y^2 is exact), and the correction
+// (1 - e)^(-3/2) = 1 + 1.5 e + 1.875 e^2 + O(e^3) applied in FP32; the result
+// is within ~1e-13 of the pull (the FP32 rounding of e ~ 2^-21 and of the
+// correction).  One FP64 operation (the float-float to double sum).  Outside
+// the exponent range the float arithmetic covers, the FP64 pull_factor
+// (m15 = 1.5 m).
+__device__ __forceinline__ double pull_factor_ff(ff x, ff m, double m15)
+{
+    const int er = ((__float_as_int(x.hi) >> 23) & 0xFF) - 127;
+    const int em = ((__float_as_int(m.hi) >> 23) & 0xFF) - 127;
+    const int ef = 2 * em - 3 * er;
+    if (er < -60 || er > 60 || ef < -180 || ef > 180 || !(x.hi > 0.0f))
+        return pull_factor(f64_of_f32(x.hi) + f64_of_f32(x.lo), m15);
+    const float y = rsqrtf(x.hi);
+    const ff y2 = ff_two_prod(y, y);
+    const ff xy2 = ff_mul(x, y2);
+    const float e = __fsub_rn(__fsub_rn(1.0f, xy2.hi), xy2.lo);
+    const float c = __fmul_rn(e, __fmaf_rn(1.875f, e, 1.5f));
+    const ff my3 = ff_mul(m, ff_mul_f(y2, y));
+    const ff fac = ff_add_f(my3, __fmul_rn(my3.hi, c));
+    return f64_of_f32(fac.hi) + f64_of_f32(fac.lo);
 }
 
 // a < b for a >= +0 (or NaN) and finite b >= +0, on the integer pipe: the

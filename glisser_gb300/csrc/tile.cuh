@@ -97,33 +97,37 @@ __device__ __forceinline__ void issue_chunk(const Common& p, const double* log, 
     bulk_copy_g2s(buf, log + (size_t)first * rec, bytes, bar);
 }
 
-// Acceleration from planet j and its encounter test (src/wh.cu:145-160):
-// the first planet inside its radius wins (flags == 0 guard).
-__device__ __forceinline__ void planet_kick(const double* L, int j, double rx, double ry, double rz, double& ax,
-                                            double& ay, double& az, uint16_t& flags, const double* s_m15,
-                                            const double* s_rh2, const uint32_t* s_id)
-{
-    double dx = rx - L[3 * j];
-    double dy = ry - L[3 * j + 1];
-    double dz = rz - L[3 * j + 2];
-    double rad = fma(dx, dx, fma(dy, dy, dz * dz));
-    if (lt_nonneg(rad, s_rh2[j]) && flags == 0) flags = (uint16_t)((s_id[j] << 8) | 0x0001);
-    double fac = pull_factor(rad, s_m15[j]);
-    ax = fma(-dx, fac, ax);
-    ay = fma(-dy, fac, ay);
-    az = fma(-dz, fac, az);
-}
-
 // Shared-memory state of one CTA.
 struct CtaShared {
     double m[MAX_PLANETS];
-    double m15[MAX_PLANETS];    // 1.5 m, the form the planet kick takes
+    double m15[MAX_PLANETS];    // 1.5 m, the FP64 planet pull's form
     double rh2[MAX_PLANETS];
+    ff mff[MAX_PLANETS];        // m and rh^2 as float-floats for the kick
+    ff rh2ff[MAX_PLANETS];
     uint32_t id[MAX_PLANETS];
     uint64_t bar[2];
     int abort;
     uint32_t item;
 };
+
+// Acceleration from planet j and its encounter test (src/wh.cu:145-160):
+// the first planet inside its radius wins (flags == 0 guard).  The
+// separation is FP64 (3 subtractions) and so is the sum into the
+// acceleration (3 FMAs); |dr|^2, the radius test and the pull factor
+// m / |dr|^3 run in float-float on the FP32 pipe (pull_factor_ff).
+__device__ __forceinline__ void planet_kick(const double* L, int j, double rx, double ry, double rz, double& ax,
+                                            double& ay, double& az, uint16_t& flags, const CtaShared& sh)
+{
+    double dx = rx - L[3 * j];
+    double dy = ry - L[3 * j + 1];
+    double dz = rz - L[3 * j + 2];
+    const ff rad = ff_add(ff_add(ff_sqr(ff_split(dx)), ff_sqr(ff_split(dy))), ff_sqr(ff_split(dz)));
+    if (ff_lt(rad, sh.rh2ff[j]) && flags == 0) flags = (uint16_t)((sh.id[j] << 8) | 0x0001);
+    double fac = pull_factor_ff(rad, sh.mff[j], sh.m15[j]);
+    ax = fma(-dx, fac, ax);
+    ay = fma(-dy, fac, ay);
+    az = fma(-dz, fac, az);
+}
 
 // Integrates particles first + k*CTA + tid (k < PPT, below first + count)
 // of one system over the block, staging that system's log through the two
@@ -216,10 +220,10 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
                 if constexpr (NP > 0) {
 #pragma unroll
                     for (int j = 1; j <= NP; j++)
-                        planet_kick(L, j, rx[k], ry[k], rz[k], aax, aay, aaz, fl, sh.m15, sh.rh2, sh.id);
+                        planet_kick(L, j, rx[k], ry[k], rz[k], aax, aay, aaz, fl, sh);
                 } else {
                     for (int j = 1; j <= np; j++)
-                        planet_kick(L, j, rx[k], ry[k], rz[k], aax, aay, aaz, fl, sh.m15, sh.rh2, sh.id);
+                        planet_kick(L, j, rx[k], ry[k], rz[k], aax, aay, aaz, fl, sh);
                 }
                 const double rr = r2[k];
                 if (lt_nonneg(rr, rh2_sun)) fl = 0x0001;
@@ -303,6 +307,8 @@ __device__ __forceinline__ void load_planet_constants(CtaShared& sh, uint32_t np
         sh.m[j] = m[j];
         sh.m15[j] = 1.5 * m[j];
         sh.rh2[j] = rh[j] * rh[j];
+        sh.mff[j] = ff_split(m[j]);
+        sh.rh2ff[j] = ff_split(sh.rh2[j]);
         sh.id[j] = pid[j];
     }
 }
