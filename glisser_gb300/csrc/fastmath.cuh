@@ -205,24 +205,23 @@ __device__ __forceinline__ ff ff_split(double d)
 // with x y^2 in float-float (y^2 is exact), and the correction
 // (1 - e)^(-3/2) = 1 + 1.5 e + 1.875 e^2 + O(e^3) applied in FP32; the result
 // is within ~1e-13 of the pull (the FP32 rounding of e ~ 2^-21 and of the
-// correction).  One FP64 operation (the float-float to double sum).  Outside
+// correction).  Outside
 // the exponent range the float arithmetic covers, the FP64 pull_factor
-// (m15 = 1.5 m).
-__device__ __forceinline__ double pull_factor_ff(ff x, ff m, double m15)
+// (m15 = 1.5 m).  No FP64 operation on the float path.
+__device__ __forceinline__ ff pull_factor_ff(ff x, ff m, double m15)
 {
     const int er = ((__float_as_int(x.hi) >> 23) & 0xFF) - 127;
     const int em = ((__float_as_int(m.hi) >> 23) & 0xFF) - 127;
     const int ef = 2 * em - 3 * er;
     if (er < -60 || er > 60 || ef < -180 || ef > 180 || !(x.hi > 0.0f))
-        return pull_factor(f64_of_f32(x.hi) + f64_of_f32(x.lo), m15);
+        return ff_split(pull_factor(f64_of_f32(x.hi) + f64_of_f32(x.lo), m15));
     const float y = rsqrtf(x.hi);
     const ff y2 = ff_two_prod(y, y);
     const ff xy2 = ff_mul(x, y2);
     const float e = __fsub_rn(__fsub_rn(1.0f, xy2.hi), xy2.lo);
     const float c = __fmul_rn(e, __fmaf_rn(1.875f, e, 1.5f));
     const ff my3 = ff_mul(m, ff_mul_f(y2, y));
-    const ff fac = ff_add_f(my3, __fmul_rn(my3.hi, c));
-    return f64_of_f32(fac.hi) + f64_of_f32(fac.lo);
+    return ff_add_f(my3, __fmul_rn(my3.hi, c));
 }
 
 // a < b for a >= +0 (or NaN) and finite b >= +0, on the integer pipe: the

@@ -110,23 +110,24 @@ struct CtaShared {
     uint32_t item;
 };
 
-// Acceleration from planet j and its encounter test (src/wh.cu:145-160):
-// the first planet inside its radius wins (flags == 0 guard).  The
-// separation is FP64 (3 subtractions) and so is the sum into the
-// acceleration (3 FMAs); |dr|^2, the radius test and the pull factor
-// m / |dr|^3 run in float-float on the FP32 pipe (pull_factor_ff).
-__device__ __forceinline__ void planet_kick(const double* L, int j, double rx, double ry, double rz, double& ax,
-                                            double& ay, double& az, uint16_t& flags, const CtaShared& sh)
+// Pull of planet j, m dr / |dr|^3 with dr = r - r_j, added to the sum s,
+// and its encounter test (src/wh.cu:145-160): the first planet inside its
+// radius wins (flags == 0 guard).  All in float-float on the FP32 pipe (the
+// position r and the staged planet log as float-floats): the planet terms
+// are perturbations next to the Sun's pull, which the drift integrates in
+// FP64, and carry ~1e-13 of their own size.
+__device__ __forceinline__ void planet_kick(const ff* L, int j, ff rx, ff ry, ff rz, ff& sx, ff& sy, ff& sz,
+                                            uint16_t& flags, const CtaShared& sh)
 {
-    double dx = rx - L[3 * j];
-    double dy = ry - L[3 * j + 1];
-    double dz = rz - L[3 * j + 2];
-    const ff rad = ff_add(ff_add(ff_sqr(ff_split(dx)), ff_sqr(ff_split(dy))), ff_sqr(ff_split(dz)));
+    const ff dx = ff_add(rx, ff_neg(L[3 * j]));
+    const ff dy = ff_add(ry, ff_neg(L[3 * j + 1]));
+    const ff dz = ff_add(rz, ff_neg(L[3 * j + 2]));
+    const ff rad = ff_add(ff_add(ff_sqr(dx), ff_sqr(dy)), ff_sqr(dz));
     if (ff_lt(rad, sh.rh2ff[j]) && flags == 0) flags = (uint16_t)((sh.id[j] << 8) | 0x0001);
-    double fac = pull_factor_ff(rad, sh.mff[j], sh.m15[j]);
-    ax = fma(-dx, fac, ax);
-    ay = fma(-dy, fac, ay);
-    az = fma(-dz, fac, az);
+    const ff fac = pull_factor_ff(rad, sh.mff[j], sh.m15[j]);
+    sx = ff_add(sx, ff_mul(dx, fac));
+    sy = ff_add(sy, ff_mul(dy, fac));
+    sz = ff_add(sz, ff_mul(dz, fac));
 }
 
 // Integrates particles first + k*CTA + tid (k < PPT, below first + count)
@@ -204,11 +205,16 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
             if (b == 0) inflight0 = false;
             else inflight1 = false;
         }
-        const double* L0 = stage + b * bufstride;
         const uint32_t cfirst = c * p.chunk;
         const uint32_t steps = min(p.chunk, p.len - cfirst);
+        // the chunk's planet log as float-floats, in place (each 8-byte double
+        // becomes the 8-byte pair of floats the kick reads)
+        double* Lw = stage + b * bufstride;
+        for (uint32_t i = tid; i < steps * rec; i += CTA) reinterpret_cast<ff*>(Lw)[i] = ff_split(Lw[i]);
+        __syncthreads();
+        const ff* L0 = reinterpret_cast<const ff*>(Lw);
         for (uint32_t s = 0; s < steps; s++) {
-            const double* L = L0 + (size_t)s * rec;
+            const ff* L = L0 + (size_t)s * rec;
 #pragma unroll
             for (int k = 0; k < PPT; k++) {
                 if (flags[k] != 0) continue;
@@ -216,15 +222,19 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
                                                        mu, p.starter, p.mlp, p.tol_dt);
                 uint16_t fl = d.flags;
                 evals += d.evals;
-                double aax = L[0], aay = L[1], aaz = L[2];
+                const ff fx = ff_split(rx[k]), fy = ff_split(ry[k]), fz = ff_split(rz[k]);
+                ff sx = { 0.0f, 0.0f }, sy = { 0.0f, 0.0f }, sz = { 0.0f, 0.0f };
                 if constexpr (NP > 0) {
 #pragma unroll
-                    for (int j = 1; j <= NP; j++)
-                        planet_kick(L, j, rx[k], ry[k], rz[k], aax, aay, aaz, fl, sh);
+                    for (int j = 1; j <= NP; j++) planet_kick(L, j, fx, fy, fz, sx, sy, sz, fl, sh);
                 } else {
-                    for (int j = 1; j <= np; j++)
-                        planet_kick(L, j, rx[k], ry[k], rz[k], aax, aay, aaz, fl, sh);
+                    for (int j = 1; j <= np; j++) planet_kick(L, j, fx, fy, fz, sx, sy, sz, fl, sh);
                 }
+                // a = h0 - sum of the planets' pulls
+                const ff gx = ff_add(L[0], ff_neg(sx)), gy = ff_add(L[1], ff_neg(sy)), gz = ff_add(L[2], ff_neg(sz));
+                const double aax = f64_of_f32(gx.hi) + f64_of_f32(gx.lo);
+                const double aay = f64_of_f32(gy.hi) + f64_of_f32(gy.lo);
+                const double aaz = f64_of_f32(gz.hi) + f64_of_f32(gz.lo);
                 const double rr = r2[k];
                 if (lt_nonneg(rr, rh2_sun)) fl = 0x0001;
                 if (gt_nonneg(rr, p.outer2)) fl = 0x0002;
