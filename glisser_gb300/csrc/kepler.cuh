@@ -315,12 +315,18 @@ __device__ __forceinline__ bool kepler_newton(double& s, double dt, double r0, d
         g = gfuns(s, alpha);
         evals++;
         double f = fma(r0, g.g1, fma(u, g.g2, fma(mu, g.g3, -dt)));
-        double fp = fma(r0, g.g0, fma(u, g.g1, mu * g.g2));
         if (lt_nonneg(fabs(f), tol)) {
-            // accepted: a Newton correction is exact to O(h^2) ~ 1e-26
-            ds = -f * rcp_seed(fp);
+            // accepted: a Newton correction is exact to O(h^2) ~ 1e-26, and
+            // f' = r0 G0 + u G1 + mu G2 (the new distance, no cancellation)
+            // is needed to a few digits only: FP32 from integer-pipe casts
+            const float fpf = fmaf(f32_trunc(r0), f32_trunc(g.g0),
+                                   fmaf(f32_trunc(u), f32_trunc(g.g1), f32_trunc(mu) * f32_trunc(g.g2)));
+            const unsigned be = ((unsigned)__float_as_int(fpf) >> 23) & 0xFFu;
+            ds = -f * ((be - 1u < 253u) ? f64_of_f32(__frcp_rn(fpf))
+                                         : 1.0 / fma(r0, g.g0, fma(u, g.g1, mu * g.g2)));
             return true;
         }
+        double fp = fma(r0, g.g0, fma(u, g.g1, mu * g.g2));
         const double k = fma(-alpha, r0, mu);
         double fpp = fma(k, g.g1, u * g.g0);
         double inv_fp = rcp_fast(fp);
