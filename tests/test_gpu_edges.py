@@ -141,3 +141,41 @@ def test_ensemble_beyond_device_planet_limit_uses_host_planets():
     got = ens.particles(0)
     err = np.linalg.norm(got["r"] - want["r"], axis=1) / np.linalg.norm(want["r"], axis=1)
     assert err.max() < 1e-12
+
+
+@pytest.mark.parametrize("units", ["si", "tiny"])
+def test_units_do_not_change_the_orbits(units):
+    """The same system in SI units (metres, seconds: |dr|^2 ~ 1e24, past the
+    float-float pull's range, so its FP64 branch runs) and in units that make
+    every length 1e-6 of an au: after 512 steps the positions, rescaled, match
+    the au/day run to 1e-12 with the same flags, and the au/day run matches
+    the oracle."""
+    m, pr, pv = planets(4, seed=3)
+    el = synth.particle_elements(np.random.default_rng(8), 256, (20, 50), (0, 0.2), 10.0)
+    r, v = G.elements_to_cartesian(m[0], el)
+    Lu, Tu = (1.495978707e11, 86400.0) if units == "si" else (1e-6, 1.0)
+    runs = []
+    for L, Tt in ((1.0, 1.0), (Lu, Tu)):
+        cfg = ("Time-Step %r\nTime-Block-Size 128\nFinal-Time 1e30\nCull-Radius %r\nOuter-Limit %r\n"
+               "Input-File unused\nOutput-Folder unused\n" % (180.0 * Tt, 0.5 * L, 300.0 * L))
+        sim = G.Simulation(cfg)
+        sim.set_planets(m * L ** 3 / Tt ** 2, pr * L, pv * L / Tt)
+        sim.set_particles(r * L, v * L / Tt)
+        sim.init()
+        for _ in range(4):
+            sim.loop()
+        p = by_id(sim.particles())
+        runs.append((p["r"] / L, p["flags"]))
+    (ra, fa), (rb, fb) = runs
+    assert np.array_equal(fa, fb)
+    live = fa == 0
+    err = np.linalg.norm(ra - rb, axis=1) / np.linalg.norm(ra, axis=1)
+    assert err[live].max() < 1e-12, err[live].max()
+    ex = O.Exec(m, pr, pv, np.arange(len(m)), r, v, np.arange(len(r)), dt=180.0, tbsize=128, outer_r=300.0,
+                cull_r=0.5)
+    for _ in range(4):
+        ex.loop()
+    want = by_id(ex.particles())
+    assert np.array_equal(want["flags"], fa)
+    err = np.linalg.norm(ra - want["r"], axis=1) / np.linalg.norm(want["r"], axis=1)
+    assert err[live].max() < 1e-10
