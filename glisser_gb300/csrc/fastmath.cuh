@@ -182,6 +182,11 @@ __device__ __forceinline__ ff ff_sqr(ff a)
 __device__ __forceinline__ bool ff_lt(ff a, ff b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
 
 __device__ __forceinline__ ff ff_scale(ff a, float pow2) { return { a.hi * pow2, a.lo * pow2 }; }   // exact
+
+// 1/6 and 1/12 as float-floats (hi the nearest float, lo the nearest float
+// to the remainder: 8e-16 relative)
+__device__ __forceinline__ ff ff_sixth() { return { 1.0f / 6.0f, -4.9670538e-09f }; }
+__device__ __forceinline__ ff ff_twelfth() { return { 1.0f / 12.0f, -2.4835269e-09f }; }
 __device__ __forceinline__ ff ff_neg(ff a) { return { -a.hi, -a.lo }; }
 
 // A double as a float-float on the integer pipe: hi = d rounded toward zero

@@ -75,14 +75,6 @@ __device__ __forceinline__ void stumpff_short(double x, double& c2, double& c3)
     c3 = fma(x, fma(x, fma(x, -1.0 / 362880.0, 1.0 / 5040.0), -1.0 / 120.0), 1.0 / 6.0);
 }
 
-// c2, c3 to x^2 only: enough when |x| < 1e-4 (the x^3 terms, at most
-// 2.5e-17 in c2 and 2.8e-18 in c3, are below half an ulp of either)
-__device__ __forceinline__ void stumpff_tiny(double x, double& c2, double& c3)
-{
-    c2 = fma(x, fma(x, 1.0 / 720.0, -1.0 / 24.0), 0.5);
-    c3 = fma(x, fma(x, 1.0 / 5040.0, -1.0 / 120.0), 1.0 / 6.0);
-}
-
 __device__ __forceinline__ GFun gfuns(double s, double alpha)
 {
     double s2 = s * s;
@@ -93,8 +85,20 @@ __device__ __forceinline__ GFun gfuns(double s, double alpha)
     const unsigned lanes = __activemask();
     if (__all_sync(lanes, lt_nonneg(ax, 1e-4))) {
         // warp-uniform: every lane in this pass has a tiny argument (steps of
-        // a few thousandths of an orbit)
-        stumpff_tiny(x, c2, c3);
+        // a few thousandths of an orbit).  G3 = s^3 c3 enters Kepler's
+        // equation, the g function and G1 only as mu G3 / dt ~ tau^2 / 6 or
+        // alpha G3 / s = x c3, both below ~3e-5 here, so it is formed in
+        // float-float on the FP32 pipe (c3's x terms in FP32, 3e-13 of c3)
+        c2 = fma(x, fma(x, 1.0 / 720.0, -1.0 / 24.0), 0.5);
+        const ff sf = ff_split(s);
+        const float xf = f32_trunc(x);
+        const ff c3f = ff_add_f(ff_sixth(), xf * fmaf(xf, 1.0f / 5040.0f, -1.0f / 120.0f));
+        const ff g3f = ff_mul(ff_mul(sf, ff_sqr(sf)), c3f);
+        g.g2 = s2 * c2;
+        g.g3 = f64_of_f32(g3f.hi) + f64_of_f32(g3f.lo);
+        g.g1 = fma(-alpha, g.g3, s);
+        g.g0 = fma(-alpha, g.g2, 1.0);
+        return g;
     } else if (__all_sync(lanes, lt_nonneg(ax, 2e-3))) {
         // warp-uniform: every lane in this pass has a small argument
         stumpff_short(x, c2, c3);
@@ -256,15 +260,13 @@ __device__ __forceinline__ double starter_series(double T, double rinv, double a
     const ff t = ff_split(T), al = ff_split(alpha);
     const ff t2 = ff_mul(t, t);
     const ff X = ff_scale(ff_mul(ff_mul(ff_split(u), ff_split(rinv)), t), 0.5f);
-    const ff sixth = { 1.0f / 6.0f, -4.9670538e-09f };   // 1/6 = hi + lo to 48 bits
-    const ff twelfth = { 1.0f / 12.0f, -2.4835269e-09f };
-    const ff Y = ff_mul(ff_mul(ff_add(ff_split(mu_r), ff_neg(al)), t2), sixth);
+    const ff Y = ff_mul(ff_mul(ff_add(ff_split(mu_r), ff_neg(al)), t2), ff_sixth());
     const ff A = ff_mul(al, t2);
     // X (X (2 - 5X) - 1) + Y (5X - 1) - Z,  Z = -A X / 12
     const ff p25 = ff_add_f(ff_mul_f(X, -5.0f), 2.0f);
     const ff t1 = ff_mul(X, ff_add_f(ff_mul(X, p25), -1.0f));
     const ff t2y = ff_mul(Y, ff_add_f(ff_mul_f(X, 5.0f), -1.0f));
-    const ff t3 = ff_mul(ff_mul(A, X), twelfth);
+    const ff t3 = ff_mul(ff_mul(A, X), ff_twelfth());
     const ff low = ff_add(ff_add(t1, t2y), t3);
     float x = X.hi, y = Y.hi, a = A.hi;
     float z = (-1.0f / 12.0f) * a * x;
