@@ -29,7 +29,7 @@ int launch_batched(const glisser_particles* pa, const BatchSystems& sys, const B
         return GLISSER_E_INVALID;
     if (((uintptr_t)sys.log & 15u) != 0 || (sys.log_stride * sizeof(double)) % 16 != 0) return GLISSER_E_INVALID;
     Common p;
-    if (!fill_common(p, pa, sp, ho, npl, len)) return GLISSER_E_INVALID;
+    if (!fill_common(p, pa, sp, ho, npl, len, BATCH_LOG_CHUNK)) return GLISSER_E_INVALID;
     size_t smem = timeblock_smem_bytes(npl, (int)p.chunk);
     cudaError_t e;
     if (sp->starter == GLISSER_STARTER_LEARNED && p.mlp)

@@ -335,7 +335,7 @@ __device__ __forceinline__ void init_barriers(CtaShared& sh)
 
 
 inline bool fill_common(Common& p, const glisser_particles* pa, const glisser_step_params* sp, const glisser_handoff* ho,
-                 uint32_t npl, uint32_t len)
+                 uint32_t npl, uint32_t len, uint32_t max_chunk = LOG_CHUNK)
 {
     p.pa = *pa;
     p.npl = npl;
@@ -348,7 +348,7 @@ inline bool fill_common(Common& p, const glisser_particles* pa, const glisser_st
     p.mlp = reinterpret_cast<const MlpDev*>(sp->mlp);
     if (p.starter == STARTER_LEARNED && !p.mlp) p.starter = STARTER_SERIES;
     p.ho = *ho;
-    p.chunk = log_chunk_steps(npl);
+    p.chunk = log_chunk_steps(npl, max_chunk);
     return p.chunk >= 2;
 }
 

@@ -37,12 +37,12 @@ thread_local char g_err[256];
 
 }  // namespace
 
-uint32_t log_chunk_steps(uint32_t npl)
+uint32_t log_chunk_steps(uint32_t npl, uint32_t max_steps)
 {
-    // as many steps as fit two buffers in 200 KB, at most LOG_CHUNK, even
+    // as many steps as fit two buffers in 200 KB, at most max_steps, even
     size_t rec_bytes = 3ull * npl * sizeof(double);
     size_t fit = (200u * 1024u) / (2 * rec_bytes);
-    return (uint32_t)(fit < (size_t)LOG_CHUNK ? fit : (size_t)LOG_CHUNK) & ~1u;
+    return (uint32_t)(fit < (size_t)max_steps ? fit : (size_t)max_steps) & ~1u;
 }
 
 size_t timeblock_smem_bytes(uint32_t npl, int chunk) { return 2ull * (size_t)chunk * 3u * npl * sizeof(double); }

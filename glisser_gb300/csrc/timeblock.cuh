@@ -12,9 +12,16 @@ namespace glisser {
 // Steps per planet-log chunk staged in shared memory (even, so that every
 // chunk is a multiple of 16 bytes for the bulk copy).
 #ifndef GLISSER_LOG_CHUNK
-#define GLISSER_LOG_CHUNK 128
+#define GLISSER_LOG_CHUNK 64
 #endif
 constexpr int LOG_CHUNK = GLISSER_LOG_CHUNK;
+// The ensemble kernel restages each system's log per tile and stays with
+// longer chunks (fewer waits per tile; it is not occupancy-limited the same
+// way).
+#ifndef GLISSER_BATCH_LOG_CHUNK
+#define GLISSER_BATCH_LOG_CHUNK 128
+#endif
+constexpr int BATCH_LOG_CHUNK = GLISSER_BATCH_LOG_CHUNK;
 constexpr int MAX_PLANETS = 64;           // planets including the Sun
 // Threads per CTA of the single-system kernel (a build-time tuning knob; the
 // CTAs per SM its registers are sized for is GLISSER_TB_MIN_BLOCKS).
@@ -24,7 +31,7 @@ constexpr int MAX_PLANETS = 64;           // planets including the Sun
 constexpr int BLOCK_THREADS = GLISSER_TB_THREADS;
 
 size_t timeblock_smem_bytes(uint32_t npl, int chunk = LOG_CHUNK);
-uint32_t log_chunk_steps(uint32_t npl);
+uint32_t log_chunk_steps(uint32_t npl, uint32_t max_steps = LOG_CHUNK);
 
 // Launches one time block; validates arguments and returns a GLISSER_* code.
 const char* timeblock_error();

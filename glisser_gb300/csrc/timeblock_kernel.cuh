@@ -9,18 +9,19 @@ namespace {
 
 using namespace tile;
 
-// CTAs per SM the register allocation is sized for (FP64-pipe bound: more
-// resident warps only help cover FP64 latency).  64 threads x 8 CTAs
-// measured 0.6 % faster than 128 x 4 and 1.6 % faster than 256 x 2 on the
-// plain-giants workload (fewer warps wait at each chunk barrier).
+// CTAs per SM the register allocation is sized for.  With the planet kick
+// and the starter in float-float on the FP32 pipe, longer dependency chains
+// make resident warps count: 10 CTAs of 64 threads (with 64-step planet-log
+// chunks, so that shared memory admits them) measured 1 % faster than 8 and
+// 12, and 4 % faster than the 7 that 128-step chunks allow.
 #ifndef GLISSER_TB_MIN_BLOCKS
-#define GLISSER_TB_MIN_BLOCKS 8
+#define GLISSER_TB_MIN_BLOCKS 10
 #endif
 
 // The learned-starter kernel carries the MLP's 32 hidden activations on top
-// of the drift's registers.
+// of the drift's registers (128 per thread).
 #ifndef GLISSER_TB_MIN_BLOCKS_LEARNED
-#define GLISSER_TB_MIN_BLOCKS_LEARNED GLISSER_TB_MIN_BLOCKS
+#define GLISSER_TB_MIN_BLOCKS_LEARNED 8
 #endif
 
 template <int NP, bool LEARNED>
