@@ -58,15 +58,6 @@ __device__ __forceinline__ double rcp_fast(double x)
     return fma(y, fma(e, e, e), y);
 }
 
-// 1/x to FP32 accuracy (~2^-22 relative) with no FP64 instruction, for
-// corrections that are themselves tiny.
-__device__ __forceinline__ double rcp_seed(double x)
-{
-    int hi = __double2hiint(x);
-    if (!float_range(hi)) return 1.0 / x;
-    return widen_bits(__frcp_rn(seed_float(hi)));
-}
-
 // m x^(-3/2) from m15 = 1.5 m, for a planet's pull m dr / |dr|^3 (x = |dr|^2):
 // with the FP32 seed y of x^(-1/2) and e = 1 - x y^2,
 //   m x^(-3/2) = m y^3 (1 - e)^(-3/2) ~ m y^3 (1 + 1.5 e) = m15 y^3 (5/3 - x y^2).

@@ -212,17 +212,6 @@ __device__ __forceinline__ double starter_fp32_kepler(double dt, double r0, doub
     return ((double)x + turns * two_pi) / sa;
 }
 
-// Third-order expansion of s(dt) about s = 0:
-//   s = t/r0 - u t^2/(2 r0^3) + (u^2/(2 r0^5) - (mu - alpha r0)/(6 r0^4)) t^3
-__device__ __forceinline__ double starter_series3(double dt, double rinv, double mu, double alpha, double u, double r0)
-{
-    double tau = dt * rinv;                  // dt / r0
-    double k = mu - alpha * r0;
-    double c2 = -0.5 * u * rinv;             // coefficient of tau^2
-    double c3 = fma(0.5 * u * rinv, u * rinv, -k * rinv * (1.0 / 6.0));
-    return tau * fma(tau, fma(tau, c3, c2), 1.0);
-}
-
 // Tenth-order reversion of the time series of Kepler's equation.
 // With T = t/r0, t/r0 = s + c2 s^2 + ... + c9 s^9 where
 //   c2 = u/(2 r0), c3 = k/(6 r0), c4 = -alpha u/(24 r0), c5 = -alpha k/(120 r0),
