@@ -193,7 +193,7 @@ __device__ __forceinline__ ff ff_split(double d)
     const unsigned m = top >= 23 ? rem >> (top - 23) : rem << (23 - top);
     const int fe = ((hw >> 20) & 0x7FF) - 1023 - 52 + top + 127;   // biased exponent of lo
     const int bits = (hw & (int)0x80000000) | (fe << 23) | (int)(m & 0x7FFFFFu);
-    return { h, (rem != 0 && fe > 0) ? __int_as_float(bits) : 0.0f };
+    return { h, (rem != 0 && fe > 0 && fe < 255) ? __int_as_float(bits) : 0.0f };
 }
 
 // m x^(-3/2) for float-float x = |dr|^2 and m (a planet's pull, as
