@@ -344,10 +344,10 @@ def run_learned(G, args, rank, barrier):
     cfg = config_text(T, dt, outer=1e5)
     m, pr, pv, r, v = synth.cartesian_state("scattered-disk", args.learned_particles, seed=2000 + rank)
 
-    def make(starter, path=None):
+    def make(starter, path=None, rr=None):
         sim = G.Simulation(cfg)
         sim.set_planets(m, pr, pv)
-        sim.set_particles(r, v)
+        sim.set_particles(r if rr is None else rr, v)
         sim.set_starter(starter, path)
         sim.set_kepler_tolerance(KEPLER_TOL_SCATTERED)
         sim.init()
@@ -410,15 +410,27 @@ def run_learned(G, args, rank, barrier):
         o = np.argsort(p["id"])
         finals[name] = (p["r"][o], p["flags"][o])
         del sim
+    # the chaos floor: the series run again from positions moved by one ulp
+    sim = make(G.STARTER_SERIES, rr=np.nextafter(r, np.inf))
+    for _ in range(1 + args.learned_blocks):
+        sim.loop()
+    p = sim.particles()
+    o = np.argsort(p["id"])
+    finals["series_1ulp"] = (p["r"][o], p["flags"][o])
+    del sim
     ref_r, ref_f = finals["series"]
-    for name in ("classic", "learned"):
+    diffs = {}
+    for name in ("classic", "learned", "series_1ulp"):
         rr, ff = finals[name]
         live = (ref_f == 0) & (ff == 0)
         d = np.linalg.norm(rr - ref_r, axis=1) / np.linalg.norm(ref_r, axis=1)
-        legs[name]["rel_pos_diff_vs_series"] = {"steps": (1 + args.learned_blocks) * T,
-                                                "max": float(d[live].max()) if live.any() else None,
-                                                "q999": float(np.quantile(d[live], 0.999)) if live.any() else None}
-        legs[name]["flags_identical_to_series"] = bool(np.array_equal(ff, ref_f))
+        diffs[name] = {"steps": (1 + args.learned_blocks) * T,
+                       "max": float(d[live].max()) if live.any() else None,
+                       "q999": float(np.quantile(d[live], 0.999)) if live.any() else None,
+                       "flags_identical": bool(np.array_equal(ff, ref_f))}
+    for name in ("classic", "learned"):
+        legs[name]["rel_pos_diff_vs_series"] = {k: diffs[name][k] for k in ("steps", "max", "q999")}
+        legs[name]["flags_identical_to_series"] = diffs[name]["flags_identical"]
     # accuracy against the FP64 oracle (universal-variable drift, the
     # reference's kepu spec) on a 4096-particle sample over 1024 steps
     from oracle import oracle as O
@@ -457,6 +469,9 @@ def run_learned(G, args, rank, barrier):
                      "guess_rel_err_held_out": guess_err,
                      "loss_last": float(losses[-100:].mean()), "network": "3-32-32-1 SiLU, BF16 weights, FP32 accumulate"},
         "starters": legs,
+        "chaos_floor": dict(diffs["series_1ulp"], note="series starter from positions one ulp away: the "
+                            "spread that rounding alone reaches over these steps, against which the "
+                            "starters' rel_pos_diff_vs_series is read"),
         "learned_vs_classic": legs["learned"]["value"] / legs["classic"]["value"],
         "learned_vs_series": legs["learned"]["value"] / legs["series"]["value"],
     }
@@ -493,10 +508,10 @@ def run_history(G, args, rank, barrier):
            "Encounter-RH-Factor 3\nCull-Radius 0.5\nOuter-Limit 300\nInput-File unused\nOutput-Folder unused\n"
            % hist)
 
-    def make(starter, path=None):
+    def make(starter, path=None, rr=None):
         sim = G.Simulation(cfg)
         sim.set_planets(m, pr, pv)
-        sim.set_particles(r, v)
+        sim.set_particles(r if rr is None else rr, v)
         sim.set_starter(starter, path)
         sim.init()
         return sim

@@ -8,16 +8,22 @@
 //
 // The arithmetic is FP64 throughout.  GB300 issues FP64 at a small fraction
 // of its FP32 rate, so the solver is written to minimise FP64 instructions:
-//  * one reciprocal per Newton pass: the quartic correction is the series
-//    reversion  ds = -h - A h^2 + (B - 2A^2) h^3  (h = f/f', A = f''/2f',
-//    B = f'''/6f'), which has the same fourth-order convergence as the
-//    reference's three nested divisions;
+//  * one FP64 reciprocal per Newton pass: the quartic correction is the
+//    series reversion  ds = -h - A h^2 + (B - 2A^2) h^3  (h = f/f',
+//    A = f''/2f', B = f'''/6f'), which has the same fourth-order
+//    convergence as the reference's three nested divisions; only h is
+//    FP64, the higher-order terms are FP32;
 //  * convergence is judged on the residual at the current s, |f| < tol*dt
 //    (the reference's DANBYB test); the Newton correction computed in that
 //    same pass is then folded into the G-functions by Taylor expansion
 //    (dG3 = G2 ds, dG2 = G1 ds, dG1 = G0 ds), so the accepted solution
 //    carries an O(tol^2) error instead of O(tol) and no second Stumpff
 //    evaluation is needed for it;
+//  * a pass whose residual is above the tolerance is still accepted when
+//    the reverted correction through fifth order provably lands within it
+//    (bounds on the dropped terms and on the FP32 rounding): the
+//    correction is then folded to third order.  A starter within ~1e-4 of
+//    the root (the learned one) so needs one Stumpff evaluation, not two;
 //  * the default starter is a tenth-order reversion of the time series of
 //    Kepler's equation, accurate to ~1e-16 for steps well inside an orbit,
 //    so the residual test normally accepts it on the first evaluation: one
@@ -294,11 +300,90 @@ struct DriftResult {
     uint16_t evals;     // Stumpff evaluations spent
 };
 
-// Quartic Newton passes from s (at most KEP_NEWTON_MAX).  On acceptance
-// (|f| < tol at the current s) returns true with the G-functions at s and
-// the pending Newton correction ds = -f/f'.  |ds| < tol s there, so ds needs
-// only a few correct digits: it takes the FP32 reciprocal of f', and f'' is
-// formed only for the passes that go on.
+// Exponent field of a float in 1..253: normal, and its reciprocal normal too.
+__device__ __forceinline__ bool f32_mid_range(float x)
+{
+    return (((unsigned)__float_as_int(x) >> 23) & 0xFFu) - 1u < 253u;
+}
+
+// The Newton correction of one pass beyond its first-order term, in FP32.
+//
+// With h = f/f' and the dimensionless a = A h, b = B h^2, c = C h^3,
+// d = D h^4 (A = f''/2f', B = f'''/6f', C = f''''/24f', D = f'''''/120f'),
+// series reversion of f(s + ds) = 0 gives
+//   ds = -h (1 + a + (2a^2 - b) + (5a^3 - 5ab + c)
+//              + (14a^4 - 21a^2 b + 6ac + 3b^2 - d) + ...),
+// and for Kepler's equation f'' = k G1 + u G0, f''' = k G0 - alpha u G1
+// (k = mu - alpha r0), f'''' = -alpha f'', f''''' = -alpha f''', so
+// c = -e a / 12 and d = -e b / 20 with e = alpha h^2.
+//
+// `x_step` gets the terms through b, the quartic step of a pass that goes
+// on (its result is judged by the next pass, so FP32 suffices; 0, a plain
+// Newton step, when h or f' is outside the float range).  The return value
+// is NEWTON_PREDICTED when the correction through d, `x_root`, already
+// lands within the tolerance, so that this pass is accepted without another
+// Stumpff evaluation ("predicted acceptance"); NEWTON_STEP for a quartic
+// step; NEWTON_WILD when |x_step| > 1 or is not finite: the start is outside
+// the basin where the reverted series means anything.
+// With rho = max(|a|, |b|^1/2, |e|^1/2) bounding every term of order n by
+// about (6 rho)^n, that needs (i) rho <= 1/24 and (6 rho)^5 <= eps/8, the
+// dropped tail against eps = tol/|f|, the tolerance in units of h, and
+// (ii) the FP32 error of x_root below eps/4: the inputs are truncated to
+// 2^-23 and k cancels, so |a| and |b| are bounded through the absolute
+// values of their terms (aa, bb) and 2^-19 (aa + bb) <= eps/4 is asked.
+// A product that underflows in FP32 only drops a term when |h/f'| and
+// |h^2/f'| stay below 2^64, which (iii) asks; overflow and NaN fail (i).
+enum NewtonPass : int { NEWTON_STEP = 0, NEWTON_PREDICTED = 1, NEWTON_WILD = 2 };
+
+__device__ __forceinline__ int newton_terms(double f, double fp, double h, double r0, double u, double mu,
+                                            double alpha, const GFun& g, double tol, float& x_step, float& x_root)
+{
+    x_step = 0.0f;
+    x_root = 0.0f;
+    const float hf = f32_trunc(h), fpf = f32_trunc(fp);
+    if (!(f32_mid_range(hf) && f32_mid_range(fpf))) return NEWTON_STEP;
+    const float hr = hf * __frcp_rn(fpf);                 // h / f'
+    const float hr2 = hr * hf;                            // h^2 / f'
+    const float uf = f32_trunc(u), af = f32_trunc(alpha), r0f = f32_trunc(r0), muf = f32_trunc(mu);
+    const float gf0 = f32_trunc(g.g0), gf1 = f32_trunc(g.g1);
+    const float ar = af * r0f, kf = muf - ar, ua = uf * af;
+    const float a = 0.5f * hr * fmaf(kf, gf1, uf * gf0);
+    const float b = (1.0f / 6.0f) * hr2 * fmaf(kf, gf0, -ua * gf1);
+    const float x2 = fmaf(2.0f * a, a, a - b);
+    if (!(fabsf(x2) <= 1.0f)) return NEWTON_WILD;
+    x_step = x2;
+    const float e = af * hf * hf;
+    const float c = (-1.0f / 12.0f) * e * a;
+    const float d = (-1.0f / 20.0f) * e * b;
+    const float a2 = a * a;
+    const float x3 = fmaf(a, fmaf(5.0f, a2, -5.0f * b), c);
+    const float x4 = fmaf(a2, fmaf(14.0f, a2, -21.0f * b), fmaf(6.0f * a, c, fmaf(3.0f * b, b, -d)));
+    x_root = x2 + (x3 + x4);
+    const float aa = 0.5f * fabsf(hr) * fmaf(fabsf(ar) + fabsf(muf), fabsf(gf1), fabsf(uf * gf0));
+    const float bb = (1.0f / 6.0f) * fabsf(hr2) * fmaf(fabsf(ar) + fabsf(muf), fabsf(gf0), fabsf(ua * gf1));
+    const float rho = fmaxf(aa, sqrtf(fmaxf(bb, fabsf(e))));
+    const float eps = f32_trunc(tol) * __frcp_rn(fabsf(f32_trunc(f)));
+    const float p = 6.0f * rho, p2 = p * p;
+    const bool predicted = rho <= (1.0f / 24.0f) && p2 * p2 * p <= 0.125f * eps &&
+                           (aa + bb) * 0x1p-19f <= 0.25f * eps && fabsf(hr) <= 0x1p64f && fabsf(hr2) <= 0x1p64f;
+    return predicted ? NEWTON_PREDICTED : NEWTON_STEP;
+}
+
+// Quartic Newton passes from s (at most KEP_NEWTON_MAX; a pass whose
+// quartic step is wild ends them, s left at the last evaluated point for the
+// Laguerre fallback).  On acceptance
+// returns true with G-functions g and a pending correction ds such that the
+// first-order fold (G3 + ds G2, G2 + ds G1, G1 + ds G0) gives the
+// G-functions at the root s + ds:
+//   - residual test, |f| < tol at the current s: g = G(s) and ds = -f/f',
+//     |ds| < tol s, so ds needs only a few correct digits (the FP32
+//     reciprocal of f') and the fold's dropped ds^2 terms are ~1e-26;
+//   - predicted acceptance (newton_terms): ds is the whole reverted
+//     correction, and g carries its second- and third-order Taylor terms,
+//     G0 - alpha ds/2 (G1 + ds/3 G0), G2 + ds^2/2 (G0 - alpha ds/3 G1),
+//     G3 + ds^2/2 (G1 - 2 ds/3 G0), which the fold completes to
+//     G(s + ds) through ds^3 (G0' = -alpha G1, G1' = G0, G2' = G1,
+//     G3' = G2); the dropped terms are below ~(ds/s)^4 ~ 1e-16 of G.
 __device__ __forceinline__ bool kepler_newton(double& s, double dt, double r0, double u, double mu, double alpha,
                                               double tol, GFun& g, double& ds, uint16_t& evals)
 {
@@ -312,22 +397,25 @@ __device__ __forceinline__ bool kepler_newton(double& s, double dt, double r0, d
             // is needed to a few digits only: FP32 from integer-pipe casts
             const float fpf = fmaf(f32_trunc(r0), f32_trunc(g.g0),
                                    fmaf(f32_trunc(u), f32_trunc(g.g1), f32_trunc(mu) * f32_trunc(g.g2)));
-            const unsigned be = ((unsigned)__float_as_int(fpf) >> 23) & 0xFFu;
-            ds = -f * ((be - 1u < 253u) ? f64_of_f32(__frcp_rn(fpf))
-                                         : 1.0 / fma(r0, g.g0, fma(u, g.g1, mu * g.g2)));
+            ds = -f * (f32_mid_range(fpf) ? f64_of_f32(__frcp_rn(fpf))
+                                          : 1.0 / fma(r0, g.g0, fma(u, g.g1, mu * g.g2)));
             return true;
         }
-        double fp = fma(r0, g.g0, fma(u, g.g1, mu * g.g2));
-        const double k = fma(-alpha, r0, mu);
-        double fpp = fma(k, g.g1, u * g.g0);
-        double inv_fp = rcp_fast(fp);
-        double h = f * inv_fp;
-        double fppp = fma(k, g.g0, -(u * alpha) * g.g1);
-        double q = fpp * inv_fp;                      // 2A
-        double p = fppp * inv_fp;                     // 6B
-        // quartic step: ds = -h (1 + A h - (B - 2A^2) h^2)
-        double corr = fma(h, fma(-h, fma(p, 1.0 / 6.0, -0.5 * q * q), 0.5 * q), 1.0);
-        s = fma(-h, corr, s);
+        const double fp = fma(r0, g.g0, fma(u, g.g1, mu * g.g2));
+        const double h = f * rcp_fast(fp);
+        float x_step, x_root;
+        const int pass = newton_terms(f, fp, h, r0, u, mu, alpha, g, tol, x_step, x_root);
+        if (pass == NEWTON_WILD) return false;
+        if (pass == NEWTON_PREDICTED) {
+            ds = fma(-h, f64_of_f32(x_root), -h);
+            const double t = ds * (1.0 / 3.0), hd = 0.5 * ds, dsh = ds * hd;
+            const double q1 = fma(t, g.g0, g.g1);
+            g.g3 = fma(dsh, fma(-2.0 * t, g.g0, g.g1), g.g3);
+            g.g2 = fma(dsh, fma(-alpha * t, g.g1, g.g0), g.g2);
+            g.g0 = fma(-alpha * hd, q1, g.g0);
+            return true;
+        }
+        s = fma(-h, f64_of_f32(x_step), s - h);
     }
     return false;
 }
