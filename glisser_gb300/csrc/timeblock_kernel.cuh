@@ -19,9 +19,11 @@ using namespace tile;
 #endif
 
 // The learned-starter kernel carries the MLP's 32 hidden activations on top
-// of the drift's registers (128 per thread).
+// of the drift's registers.  A bound of 7 CTAs per SM (ptxas still picks 128
+// registers, spilling 96 bytes) measured 1.6 % faster than 8 (128, 136
+// bytes spilled) and 8 % faster than 6 or 9.
 #ifndef GLISSER_TB_MIN_BLOCKS_LEARNED
-#define GLISSER_TB_MIN_BLOCKS_LEARNED 8
+#define GLISSER_TB_MIN_BLOCKS_LEARNED 7
 #endif
 
 template <int NP, bool LEARNED>
