@@ -196,6 +196,29 @@ __device__ __forceinline__ ff ff_split(double d)
     return { h, (rem != 0 && fe > 0 && fe < 255) ? __int_as_float(bits) : 0.0f };
 }
 
+// hi + lo of a float-float as a double, on the integer pipe: hi widened
+// exactly, then lo's significand added to (or, lo of the other sign, taken
+// from) the magnitude bits in units of the double's last place -- one place
+// finer when hi is a power of two and the result falls into the binade below
+// -- with the bits below that place dropped.  |lo| < ulp(hi) keeps the sum
+// inside hi's binade (or the one below), so no carry reaches the exponent
+// unaccounted for.  Within one unit in the last place of the exact sum (the
+// FP64 addition it replaces is within half).  Pairs outside that form (hi
+// below 2^-67, not finite, or |lo| >= ulp(hi)) take the FP64 addition.
+__device__ __forceinline__ double ff_to_f64(ff x)
+{
+    const int hb = __float_as_int(x.hi), lb = __float_as_int(x.lo);
+    const int eh = (hb >> 23) & 0xFF, el = (lb >> 23) & 0xFF;
+    if ((unsigned)(eh - 60) > 193u || el > eh - 24) return f64_of_f32(x.hi) + f64_of_f32(x.lo);
+    const long long d = __double_as_longlong(widen_bits(x.hi));
+    const bool opp = (hb ^ lb) < 0;
+    const int sh = el - eh + 29 + ((opp && (hb & 0x7FFFFF) == 0) ? 1 : 0);
+    const unsigned ml = (unsigned)((lb & 0x7FFFFF) | 0x800000);
+    unsigned dl = sh >= 0 ? ml << sh : ml >> min(-sh, 31);
+    dl = el != 0 ? dl : 0u;                      // lo zero (or subnormal: below 2^-59 of hi)
+    return __longlong_as_double(opp ? d - (long long)dl : d + (long long)dl);
+}
+
 // m x^(-3/2) for float-float x = |dr|^2 and m (a planet's pull, as
 // pull_factor), on the FP32 pipe: the seed y = rsqrtf(x.hi), e = 1 - x y^2
 // with x y^2 in float-float (y^2 is exact), and the correction

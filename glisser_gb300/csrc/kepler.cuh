@@ -101,7 +101,7 @@ __device__ __forceinline__ GFun gfuns(double s, double alpha)
         const ff c3f = ff_add_f(ff_sixth(), xf * fmaf(xf, 1.0f / 5040.0f, -1.0f / 120.0f));
         const ff g3f = ff_mul(ff_mul(sf, ff_sqr(sf)), c3f);
         g.g2 = s2 * c2;
-        g.g3 = f64_of_f32(g3f.hi) + f64_of_f32(g3f.lo);
+        g.g3 = ff_to_f64(g3f);
         g.g1 = fma(-alpha, g.g3, s);
         g.g0 = fma(-alpha, g.g2, 1.0);
         return g;
@@ -292,7 +292,7 @@ __device__ __forceinline__ double starter_series(double T, double rinv, double a
     float r3c = fmaf(4.0f / 945.0f, x2, -23.0f / 75600.0f * y);
     float o10 = 11.0f * x * fmaf(a, fmaf(a, fmaf(a, r3c, r2c), r1c), r0c);
     const ff sum = ff_add_f(low, ((o5 + o6) + (o7 + o8)) + (o9 + o10));
-    return fma(T, f64_of_f32(sum.hi) + f64_of_f32(sum.lo), T);
+    return fma(T, ff_to_f64(sum), T);
 }
 
 struct DriftResult {

@@ -232,9 +232,19 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
                 }
                 // a = h0 - sum of the planets' pulls
                 const ff gx = ff_add(L[0], ff_neg(sx)), gy = ff_add(L[1], ff_neg(sy)), gz = ff_add(L[2], ff_neg(sz));
-                const double aax = f64_of_f32(gx.hi) + f64_of_f32(gx.lo);
-                const double aay = f64_of_f32(gy.hi) + f64_of_f32(gy.lo);
-                const double aaz = f64_of_f32(gz.hi) + f64_of_f32(gz.lo);
+                // to FP64 on the integer pipe where the FP64 pipe is the bound; the
+                // learned kernel, bound by the network's FP32 work and issue,
+                // measured faster with the FP64 addition
+                double aax, aay, aaz;
+                if constexpr (LEARNED) {
+                    aax = f64_of_f32(gx.hi) + f64_of_f32(gx.lo);
+                    aay = f64_of_f32(gy.hi) + f64_of_f32(gy.lo);
+                    aaz = f64_of_f32(gz.hi) + f64_of_f32(gz.lo);
+                } else {
+                    aax = ff_to_f64(gx);
+                    aay = ff_to_f64(gy);
+                    aaz = ff_to_f64(gz);
+                }
                 const double rr = r2[k];
                 if (lt_nonneg(rr, rh2_sun)) fl = 0x0001;
                 if (gt_nonneg(rr, p.outer2)) fl = 0x0002;
