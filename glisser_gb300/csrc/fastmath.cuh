@@ -219,6 +219,28 @@ __device__ __forceinline__ double ff_to_f64(ff x)
     return __longlong_as_double(opp ? d - (long long)dl : d + (long long)dl);
 }
 
+// d + c on the integer pipe for a correction c below 2^-28 of d's binade
+// (past a float's precision of d): c's significand, aligned to d's last
+// place with the bits below it dropped, added to (or, opposite signs, taken
+// from) d's magnitude bits.  Within one unit in d's last place of the exact
+// sum (the FP64 addition it replaces is within half of the result's).  A
+// zero or subnormal c leaves d; d not normal, a larger c, or a sum that
+// leaves d's binade take the FP64 addition.
+__device__ __forceinline__ double f64_add_tiny(double d, float c)
+{
+    const long long db = __double_as_longlong(d);
+    const int cb = __float_as_int(c);
+    const int ed = (int)((unsigned long long)db >> 52) & 0x7FF, ec = (cb >> 23) & 0xFF;
+    if (ec == 0) return d;
+    const int sh = ec - ed + (1075 - 150);       // c = ml 2^(ec-150), d's last place 2^(ed-1075)
+    if (sh > 0 || ed == 0 || ed == 0x7FF) return d + f64_of_f32(c);
+    const unsigned ml = (unsigned)((cb & 0x7FFFFF) | 0x800000);
+    const unsigned dl = ml >> min(-sh, 31);
+    const long long r = ((db ^ ((long long)cb << 32)) < 0) ? db - (long long)dl : db + (long long)dl;
+    if (((r ^ db) >> 52) != 0) return d + f64_of_f32(c);
+    return __longlong_as_double(r);
+}
+
 // m x^(-3/2) for float-float x = |dr|^2 and m (a planet's pull, as
 // pull_factor), on the FP32 pipe: the seed y = rsqrtf(x.hi), e = 1 - x y^2
 // with x y^2 in float-float (y^2 is exact), and the correction

@@ -52,9 +52,13 @@ enum Starter : int {
     STARTER_LEARNED = 2,   // MLP over drift invariants, classic fallback
 };
 
+// G1, G2, G3 of one Stumpff evaluation; G0 = 1 - alpha G2 is formed where a
+// pass needs it (gfun_g0), in FP64 or FP32.
 struct GFun {
-    double g0, g1, g2, g3;
+    double g1, g2, g3;
 };
+
+__device__ __forceinline__ double gfun_g0(const GFun& g, double alpha) { return fma(-alpha, g.g2, 1.0); }
 
 // Stumpff c2(x), c3(x) series coefficients: (-1)^k/(2k+2)! and (-1)^k/(2k+3)!
 __device__ __forceinline__ void stumpff_small(double x, double& c2, double& c3)
@@ -81,6 +85,12 @@ __device__ __forceinline__ void stumpff_short(double x, double& c2, double& c3)
     c3 = fma(x, fma(x, fma(x, -1.0 / 362880.0, 1.0 / 5040.0), -1.0 / 120.0), 1.0 / 6.0);
 }
 
+// FP64_BOUND (here and in the solver below): the kernel is bound by the
+// FP64 pipe, so float-to-double sums and the residual-accepted fold go
+// through the integer pipe (ff_to_f64, f64_add_tiny); otherwise (the learned
+// kernels, bound by the network's FP32 work and issue, with no registers to
+// spare) they stay FP64 additions, which measured faster there.
+template <bool FP64_BOUND>
 __device__ __forceinline__ GFun gfuns(double s, double alpha)
 {
     double s2 = s * s;
@@ -101,9 +111,8 @@ __device__ __forceinline__ GFun gfuns(double s, double alpha)
         const ff c3f = ff_add_f(ff_sixth(), xf * fmaf(xf, 1.0f / 5040.0f, -1.0f / 120.0f));
         const ff g3f = ff_mul(ff_mul(sf, ff_sqr(sf)), c3f);
         g.g2 = s2 * c2;
-        g.g3 = ff_to_f64(g3f);
+        g.g3 = FP64_BOUND ? ff_to_f64(g3f) : f64_of_f32(g3f.hi) + f64_of_f32(g3f.lo);
         g.g1 = fma(-alpha, g.g3, s);
-        g.g0 = fma(-alpha, g.g2, 1.0);
         return g;
     } else if (__all_sync(lanes, lt_nonneg(ax, 2e-3))) {
         // warp-uniform: every lane in this pass has a small argument
@@ -127,18 +136,15 @@ __device__ __forceinline__ GFun gfuns(double s, double alpha)
             c1 = c0 * c1;
             c0 = fma(2.0 * c0, c0, -1.0);
         }
-        g.g0 = c0;
         g.g1 = s * c1;
         g.g2 = s2 * c2;
         g.g3 = s2 * s * c3;
         return g;
     }
-    // c1 = 1 - x c3 and c0 = 1 - x c2 folded into G1 = s - alpha G3 and
-    // G0 = 1 - alpha G2
+    // c1 = 1 - x c3 folded into G1 = s - alpha G3
     g.g2 = s2 * c2;
     g.g3 = s * (s2 * c3);
     g.g1 = fma(-alpha, g.g3, s);
-    g.g0 = fma(-alpha, g.g2, 1.0);
     return g;
 }
 
@@ -336,7 +342,8 @@ __device__ __forceinline__ bool f32_mid_range(float x)
 enum NewtonPass : int { NEWTON_STEP = 0, NEWTON_PREDICTED = 1, NEWTON_WILD = 2 };
 
 __device__ __forceinline__ int newton_terms(double f, double fp, double h, double r0, double u, double mu,
-                                            double alpha, const GFun& g, double tol, float& x_step, float& x_root)
+                                            double alpha, double g0, const GFun& g, double tol, float& x_step,
+                                            float& x_root)
 {
     x_step = 0.0f;
     x_root = 0.0f;
@@ -345,7 +352,7 @@ __device__ __forceinline__ int newton_terms(double f, double fp, double h, doubl
     const float hr = hf * __frcp_rn(fpf);                 // h / f'
     const float hr2 = hr * hf;                            // h^2 / f'
     const float uf = f32_trunc(u), af = f32_trunc(alpha), r0f = f32_trunc(r0), muf = f32_trunc(mu);
-    const float gf0 = f32_trunc(g.g0), gf1 = f32_trunc(g.g1);
+    const float gf0 = f32_trunc(g0), gf1 = f32_trunc(g.g1);
     const float ar = af * r0f, kf = muf - ar, ua = uf * af;
     const float a = 0.5f * hr * fmaf(kf, gf1, uf * gf0);
     const float b = (1.0f / 6.0f) * hr2 * fmaf(kf, gf0, -ua * gf1);
@@ -369,50 +376,82 @@ __device__ __forceinline__ int newton_terms(double f, double fp, double h, doubl
     return predicted ? NEWTON_PREDICTED : NEWTON_STEP;
 }
 
+// The residual-accepted correction folded into the G-functions to first
+// order, G3 + ds G2, G2 + ds G1, G1 + ds G0: |ds| < tol s, so each term is
+// below ~3 tol of the G-function it corrects and needs only a float's
+// precision -- the products are FP32 and enter through f64_add_tiny (the
+// FP64 fold when ds or a product is outside the float range).
+template <bool FP64_BOUND>
+__device__ __forceinline__ void fold_small(GFun& g, double& ds, double f, double r0, double u, double mu,
+                                           double alpha)
+{
+    const float g1f = f32_trunc(g.g1), g2f = f32_trunc(g.g2), af = f32_trunc(alpha);
+    const float g0f = fmaf(-af, g2f, 1.0f);
+    const float fpf = fmaf(f32_trunc(r0), g0f, fmaf(f32_trunc(u), g1f, f32_trunc(mu) * g2f));
+    const float dsf = -f32_trunc(f) * __frcp_rn(fpf);
+    const float c3 = dsf * g2f, c2 = dsf * g1f, c1 = dsf * g0f;
+    if (f32_mid_range(fpf) && f32_mid_range(c3) && f32_mid_range(c2) && f32_mid_range(c1)) {
+        ds = f64_of_f32(dsf);
+        if constexpr (FP64_BOUND) {
+            g.g3 = f64_add_tiny(g.g3, c3);
+            g.g2 = f64_add_tiny(g.g2, c2);
+            g.g1 = f64_add_tiny(g.g1, c1);
+        } else {
+            g.g3 += f64_of_f32(c3);
+            g.g2 += f64_of_f32(c2);
+            g.g1 += f64_of_f32(c1);
+        }
+    } else {
+        const double g0 = gfun_g0(g, alpha);
+        ds = -f / fma(r0, g0, fma(u, g.g1, mu * g.g2));
+        g.g3 = fma(ds, g.g2, g.g3);
+        g.g2 = fma(ds, g.g1, g.g2);
+        g.g1 = fma(ds, g0, g.g1);
+    }
+}
+
 // Quartic Newton passes from s (at most KEP_NEWTON_MAX; a pass whose
 // quartic step is wild ends them, s left at the last evaluated point for the
-// Laguerre fallback).  On acceptance
-// returns true with G-functions g and a pending correction ds such that the
-// first-order fold (G3 + ds G2, G2 + ds G1, G1 + ds G0) gives the
-// G-functions at the root s + ds:
-//   - residual test, |f| < tol at the current s: g = G(s) and ds = -f/f',
-//     |ds| < tol s, so ds needs only a few correct digits (the FP32
-//     reciprocal of f') and the fold's dropped ds^2 terms are ~1e-26;
+// Laguerre fallback).  On acceptance returns true with the G-functions at
+// the root s + ds in g:
+//   - residual test, |f| < tol at the current s: ds = -f/f' folded to first
+//     order (fold_small); the dropped ds^2 terms are ~1e-26 of G, so the
+//     accepted solution carries an O(tol^2) error instead of O(tol);
 //   - predicted acceptance (newton_terms): ds is the whole reverted
-//     correction, and g carries its second- and third-order Taylor terms,
-//     G0 - alpha ds/2 (G1 + ds/3 G0), G2 + ds^2/2 (G0 - alpha ds/3 G1),
-//     G3 + ds^2/2 (G1 - 2 ds/3 G0), which the fold completes to
-//     G(s + ds) through ds^3 (G0' = -alpha G1, G1' = G0, G2' = G1,
-//     G3' = G2); the dropped terms are below ~(ds/s)^4 ~ 1e-16 of G.
+//     correction, folded by Taylor expansion through ds^3 (G0' = -alpha G1,
+//     G1' = G0, G2' = G1, G3' = G2):
+//       G3 + ds (G2 + ds/2 (G1 + ds/3 G0)),
+//       G2 + ds (G1 + ds/2 (G0 - alpha ds/3 G1)),
+//       G1 + ds (G0 - alpha ds/2 (G1 + ds/3 G0));
+//     the dropped terms are below ~(ds/s)^4 ~ 1e-16 of G.
+template <bool FP64_BOUND>
 __device__ __forceinline__ bool kepler_newton(double& s, double dt, double r0, double u, double mu, double alpha,
                                               double tol, GFun& g, double& ds, uint16_t& evals)
 {
     for (int it = 0; it < KEP_NEWTON_MAX; it++) {
-        g = gfuns(s, alpha);
+        g = gfuns<FP64_BOUND>(s, alpha);
         evals++;
         double f = fma(r0, g.g1, fma(u, g.g2, fma(mu, g.g3, -dt)));
         if (lt_nonneg(fabs(f), tol)) {
-            // accepted: a Newton correction is exact to O(h^2) ~ 1e-26, and
-            // f' = r0 G0 + u G1 + mu G2 (the new distance, no cancellation)
-            // is needed to a few digits only: FP32 from integer-pipe casts
-            const float fpf = fmaf(f32_trunc(r0), f32_trunc(g.g0),
-                                   fmaf(f32_trunc(u), f32_trunc(g.g1), f32_trunc(mu) * f32_trunc(g.g2)));
-            ds = -f * (f32_mid_range(fpf) ? f64_of_f32(__frcp_rn(fpf))
-                                          : 1.0 / fma(r0, g.g0, fma(u, g.g1, mu * g.g2)));
+            fold_small<FP64_BOUND>(g, ds, f, r0, u, mu, alpha);
             return true;
         }
-        const double fp = fma(r0, g.g0, fma(u, g.g1, mu * g.g2));
+        const double g0 = gfun_g0(g, alpha);
+        const double fp = fma(r0, g0, fma(u, g.g1, mu * g.g2));
         const double h = f * rcp_fast(fp);
         float x_step, x_root;
-        const int pass = newton_terms(f, fp, h, r0, u, mu, alpha, g, tol, x_step, x_root);
+        const int pass = newton_terms(f, fp, h, r0, u, mu, alpha, g0, g, tol, x_step, x_root);
         if (pass == NEWTON_WILD) return false;
         if (pass == NEWTON_PREDICTED) {
             ds = fma(-h, f64_of_f32(x_root), -h);
-            const double t = ds * (1.0 / 3.0), hd = 0.5 * ds, dsh = ds * hd;
-            const double q1 = fma(t, g.g0, g.g1);
-            g.g3 = fma(dsh, fma(-2.0 * t, g.g0, g.g1), g.g3);
-            g.g2 = fma(dsh, fma(-alpha * t, g.g1, g.g0), g.g2);
-            g.g0 = fma(-alpha * hd, q1, g.g0);
+            const double t = ds * (1.0 / 3.0), hd = 0.5 * ds;
+            const double q1 = fma(t, g0, g.g1);
+            const double n3 = fma(ds, fma(hd, q1, g.g2), g.g3);
+            const double n2 = fma(ds, fma(hd, fma(-alpha * t, g.g1, g0), g.g1), g.g2);
+            const double n1 = fma(ds, fma(-alpha * hd, q1, g0), g.g1);
+            g.g3 = n3;
+            g.g2 = n2;
+            g.g1 = n1;
             return true;
         }
         s = fma(-h, f64_of_f32(x_step), s - h);
@@ -422,20 +461,26 @@ __device__ __forceinline__ bool kepler_newton(double& s, double dt, double r0, d
 
 // Laguerre's method (n = 5) from s (SWIFT drift_kepu_lag, with the exact
 // f'' = (mu - alpha r0) G1 + u G0), at most KEP_LAGUERRE_MAX passes; same
-// outputs as kepler_newton.
+// outputs as kepler_newton (the accepted correction folded to first order in
+// FP64).
+template <bool FP64_BOUND>
 __device__ __forceinline__ bool kepler_laguerre(double& s, double dt, double r0, double u, double mu, double alpha,
                                              double tol, GFun& g, double& ds, uint16_t& evals)
 {
     const double ln = 5.0;
     const double k = fma(-alpha, r0, mu);
     for (int it = 0; it < KEP_LAGUERRE_MAX; it++) {
-        g = gfuns(s, alpha);
+        g = gfuns<FP64_BOUND>(s, alpha);
         evals++;
+        const double g0 = gfun_g0(g, alpha);
         double f = fma(r0, g.g1, fma(u, g.g2, fma(mu, g.g3, -dt)));
-        double fp = fma(r0, g.g0, fma(u, g.g1, mu * g.g2));
-        double fpp = fma(k, g.g1, u * g.g0);
+        double fp = fma(r0, g0, fma(u, g.g1, mu * g.g2));
+        double fpp = fma(k, g.g1, u * g0);
         if (fabs(f) < tol) {
             ds = -f / fp;
+            g.g3 = fma(ds, g.g2, g.g3);
+            g.g2 = fma(ds, g.g1, g.g2);
+            g.g1 = fma(ds, g0, g.g1);
             return true;
         }
         double disc = sqrt(fabs((ln - 1.0) * (ln - 1.0) * fp * fp - (ln - 1.0) * ln * f * fpp));
@@ -488,24 +533,17 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
     const double tol = tol_dt;
     GFun g;
     double ds = 0;
-    bool ok = kepler_newton(s, dt, r0, u, mu, alpha, tol, g, ds, res.evals);
+    bool ok = kepler_newton<!LEARNED>(s, dt, r0, u, mu, alpha, tol, g, ds, res.evals);
     if constexpr (LEARNED) {
         if (!ok && from_mlp) {
             s = starter_classic(dt, r0, rinv, mu, alpha, u);
-            ok = kepler_newton(s, dt, r0, u, mu, alpha, tol, g, ds, res.evals);
+            ok = kepler_newton<!LEARNED>(s, dt, r0, u, mu, alpha, tol, g, ds, res.evals);
         }
     }
-    if (!ok) ok = kepler_laguerre(s, dt, r0, u, mu, alpha, tol, g, ds, res.evals);
-    if (!ok) {
-        res.flags |= 0x04;
-        ds = 0;
-    }
-    // fold the last correction into the G-functions (dG3 = G2 ds, dG2 =
-    // G1 ds, dG1 = G0 ds; |ds| < 1e-13 s, so the second-order terms are
-    // below 1e-26)
-    double g3 = fma(ds, g.g2, g.g3);
-    double g2 = fma(ds, g.g1, g.g2);
-    double g1 = fma(ds, g.g0, g.g1);
+    if (!ok) ok = kepler_laguerre<!LEARNED>(s, dt, r0, u, mu, alpha, tol, g, ds, res.evals);
+    if (!ok) res.flags |= 0x04;
+    // g: the G-functions at the root (the last evaluation's when not converged)
+    const double g3 = g.g3, g2 = g.g2, g1 = g.g1;
 
     double ff = fma(-mu_r, g2, 1.0);
     double gg = fma(-mu, g3, dt);

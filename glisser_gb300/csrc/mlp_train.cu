@@ -74,8 +74,8 @@ __global__ void log_solves_kernel(glisser_particles pa, uint32_t n, double dt, d
         GFun g;
         double ds = 0;
         uint16_t ev = 0;
-        bool ok = kepler_newton(s, dt, r0, u, mu, alpha, tol, g, ds, ev);
-        if (!ok) ok = kepler_laguerre(s, dt, r0, u, mu, alpha, tol, g, ds, ev);
+        bool ok = kepler_newton<true>(s, dt, r0, u, mu, alpha, tol, g, ds, ev);
+        if (!ok) ok = kepler_laguerre<true>(s, dt, r0, u, mu, alpha, tol, g, ds, ev);
         evals = ev;
         float f0, f1, f2;
         mlp_features(tau2_f32(dt * rinv, mu_r), u, rinv, mu_r, alpha, f0, f1, f2);

@@ -216,7 +216,10 @@ def test_bad_weights_file_is_rejected(tmp_path):
 
 def test_outside_the_training_box_the_classic_starter_runs(trained):
     """Drifts whose features fall outside the network's training box start
-    from the classic starter: identical iteration counts and results."""
+    from the classic starter: identical iteration counts and flags, results
+    equal to rounding (the learned kernels sum float-float values with FP64
+    additions where the FP64-bound kernels use the integer pipe, so the last
+    bit may differ)."""
     tr, _, _, _ = trained
     nm = tr.norm
     narrow = L.Trainer(16, seed=1)
@@ -225,8 +228,10 @@ def test_outside_the_training_box_the_classic_starter_runs(trained):
     m, pr, pv, r, v = synth.cartesian_state("scattered-disk", 2048, seed=14)
     a = L.drift_states(r, v, DT, m[0], G.STARTER_LEARNED, narrow)
     b = L.drift_states(r, v, DT, m[0], G.STARTER_CLASSIC)
-    assert np.array_equal(a[2], b[2])
-    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert np.array_equal(a[2], b[2]) and np.array_equal(a[3], b[3])
+    for k in (0, 1):
+        d = np.linalg.norm(a[k] - b[k], axis=1) / np.linalg.norm(b[k], axis=1)
+        assert d.max() < 1e-15, (k, d.max())
 
 
 def test_tighter_kepler_tolerance(trained):
