@@ -37,8 +37,11 @@ DRAM_BYTES_PER_PARTICLE_BLOCK = 76.6
 KEPLER_TOL_SCATTERED = 1e-14     # the scattered-disk workload's Newton tolerance
 # FP64 thread-instructions per particle-step of timeblock_kernel<4> (series
 # starter) counted by ncu (smsp__sass_thread_inst_executed_op_d{add,fma,mul}),
-# for the executed-FP64 view of the roofline
-FP64_INSTR_PER_STEP_NP4 = {"dadd": 6.5, "dfma": 36.1, "dmul": 23.1}
+# and the FP64 pipe's busy share (sm__pipe_fp64_cycles_active, pct of peak
+# sustained active) of the same capture, for the executed-FP64 view of the
+# roofline
+FP64_INSTR_PER_STEP_NP4 = {"dadd": 2.0, "dfma": 31.1, "dmul": 21.1}
+FP64_PIPE_BUSY_NP4 = 0.719
 
 
 def alg_flops_per_particle_step(n_planets, k_ref=5):
@@ -56,9 +59,12 @@ def executed_fp64_view(n_planets, rate, peak_tf):
     c = FP64_INSTR_PER_STEP_NP4
     flops = c["dadd"] + c["dmul"] + 2 * c["dfma"]
     tf = rate * flops / 1e12
-    return {"instructions_per_particle_step": sum(c.values()), "flops_per_particle_step": flops,
+    return {"instructions_per_particle_step": round(sum(c.values()), 1), "flops_per_particle_step": flops,
             "achieved": tf, "peak": peak_tf, "unit": "TFLOP/s", "frac": tf / peak_tf if peak_tf else None,
-            "source": "ncu instruction counts of timeblock_kernel<4> (profiles/timeblock_kernel_plain-giants.md)"}
+            "fp64_pipe_busy": FP64_PIPE_BUSY_NP4,
+            "source": "ncu instruction counts and FP64 pipe cycles of timeblock_kernel<4> "
+                      "(profiles/timeblock_kernel_plain-giants.md); a DADD or DMUL fills an FP64 slot with one "
+                      "flop, so frac counts flops, fp64_pipe_busy the slots"}
 
 
 def config_text(tbsize, dt, outer=300.0):
