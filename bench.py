@@ -684,7 +684,7 @@ def run_track(G, sim):
         if os.path.exists(path):
             os.remove(path)
     # dump stream: the full state back from the device (pinned staging) and
-    # the binary state file (the driver's dumps use the same calls)
+    # the binary state file (glisser_run's dumps use the same calls)
     dpath = os.path.join(d, "glisser_dump_%d.out" % os.getpid())
     try:
         sim.set_particles(*(lambda p: (p["r"], p["v"]))(sim.particles()))    # mark the host mirror stale

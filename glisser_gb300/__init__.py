@@ -129,6 +129,7 @@ def lib():
             "glisser_stats": ([P, C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong)], C.c_int),
             "glisser_elements_to_cartesian": ([C.c_size_t, C.c_double, D, D, D], C.c_int),
             "glisser_fp64_peak_probe": ([D, D], C.c_int),
+            "glisser_fastmath_check": ([C.c_size_t, P, P, P, P, P, P, P], C.c_int),
             "glisser_launches": ([P, C.POINTER(C.c_ulonglong)], C.c_int),
             "glisser_l2_flush": ([P, C.c_size_t], C.c_int),
             "glisser_wait_check": ([C.c_double, U32, D], C.c_int),
@@ -236,6 +237,26 @@ def fp64_peak_probe():
     if rc:
         _raise(rc, last_error())
     return tf.value, ms.value
+
+
+def fastmath_check(hi, lo, d, c):
+    """The particle kernel's integer-pipe sums on cuda:0: hi + lo (float-float
+    to double) and d + c (a tiny correction added to a double), elementwise
+    over host arrays; returns the two double arrays."""
+    import torch
+    dev = torch.device("cuda:0")
+    t = [torch.tensor(np.ascontiguousarray(x, dt), device=dev)
+         for x, dt in ((hi, np.float32), (lo, np.float32), (d, np.float64), (c, np.float32))]
+    n = len(t[0])
+    if any(len(x) != n for x in t):
+        raise ValueError("fastmath_check: arrays of different lengths")
+    out = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(2)]
+    rc = lib().glisser_fastmath_check(n, *[x.data_ptr() for x in t], out[0].data_ptr(), out[1].data_ptr(),
+                                      C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    if rc:
+        _raise(rc, last_error())
+    torch.cuda.synchronize()
+    return out[0].cpu().numpy(), out[1].cpu().numpy()
 
 
 def l2_flush(stream, nbytes=256 << 20):

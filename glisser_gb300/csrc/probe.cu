@@ -1,17 +1,32 @@
 // FP64 throughput probe: the denominator of the particle kernel's roofline.
 //
-// GB300's FP64 rate is a small fraction of its FP32 rate and the driver's
-// measured-peaks file has no FP64 entry, so the library measures it: every
-// thread runs 8 independent dependent chains of DFMA (enough to cover the
-// pipe latency), on a grid of 4 CTAs x 256 threads per SM, timed with CUDA
-// events.  2 flops per DFMA.
+// GB300's FP64 rate is a small fraction of its FP32 rate and the measured
+// copy-bandwidth and GEMM peaks have no FP64 entry, so the library measures
+// it: every thread runs 8 independent dependent chains of DFMA (enough to
+// cover the pipe latency), on a grid of 4 CTAs x 256 threads per SM, timed
+// with CUDA events.  2 flops per DFMA.
+//
+// Also here: glisser_fastmath_check, which runs the particle kernel's
+// integer-pipe sums (fastmath.cuh) on arrays for their tests, and the L2
+// flush of the benchmarks.
 #include <cuda_runtime.h>
 
 #include "../../include/glisser.h"
+#include "fastmath.cuh"
 
 namespace glisser {
 
 namespace {
+
+// The particle kernel's integer-pipe sums (fastmath.cuh) on device arrays.
+__global__ void fastmath_check_kernel(size_t n, const float* hi, const float* lo, const double* d, const float* c,
+                                      double* out_ff, double* out_tiny)
+{
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out_ff[i] = ff_to_f64(ff{ hi[i], lo[i] });
+    out_tiny[i] = f64_add_tiny(d[i], c[i]);
+}
 
 __global__ void __launch_bounds__(256) dfma_chains(double* out, int iters, double a, double b)
 {
@@ -77,4 +92,16 @@ extern "C" int glisser_l2_flush(void* stream, size_t bytes)
     }
     return cudaMemsetAsync(buf, (int)(bytes & 0xFF), bytes, (cudaStream_t)stream) == cudaSuccess ? GLISSER_OK
                                                                                                  : GLISSER_E_CUDA;
+}
+
+extern "C" int glisser_fastmath_check(size_t n, const float* hi, const float* lo, const double* d, const float* c,
+                                      double* out_ff, double* out_tiny, void* stream)
+{
+    if (n == 0) return GLISSER_OK;
+    if (!hi || !lo || !d || !c || !out_ff || !out_tiny) return GLISSER_E_INVALID;
+    const unsigned threads = 256;
+    const unsigned blocks = (unsigned)((n + threads - 1) / threads);
+    if ((size_t)blocks * threads < n) return GLISSER_E_INVALID;
+    glisser::fastmath_check_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(n, hi, lo, d, c, out_ff, out_tiny);
+    return cudaGetLastError() == cudaSuccess ? GLISSER_OK : GLISSER_E_CUDA;
 }

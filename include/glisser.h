@@ -359,6 +359,12 @@ int glisser_elements_to_cartesian(size_t n, double mu, const double *el6, double
  * short probe kernel; *ms receives its duration.  No reference counterpart:
  * it is the denominator of the particle kernel's roofline. */
 int glisser_fp64_peak_probe(double *tflops, double *ms);
+/* Runs the particle kernel's integer-pipe sums on n device elements, for
+ * their tests: out_ff[i] = hi[i] + lo[i] (a normalised float-float pair) and
+ * out_tiny[i] = d[i] + c[i] (c far below d), each as the kernel forms it.
+ * No reference counterpart. */
+int glisser_fastmath_check(size_t n, const float *hi, const float *lo, const double *d, const float *c,
+                           double *out_ff, double *out_tiny, void *stream);
 /* Overwrites `bytes` of a library-owned scratch buffer on `stream` (a
  * cudaStream_t) so the next kernel starts with a cold L2; benchmark hygiene,
  * no reference counterpart. */
