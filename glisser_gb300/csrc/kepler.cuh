@@ -489,43 +489,57 @@ __device__ __forceinline__ bool kepler_laguerre(double& s, double dt, double r0,
     return false;
 }
 
-// Drifts (r, v) by dt about a central mass mu.  r2 = |r|^2 and rinv = 1/|r|
-// come in for the state and go out for the new position, both taken from the
-// new position vector itself (its length enters the energy alpha = 2 mu / r0
-// - v^2 of the next drift, where near pericentre of an eccentric orbit any
-// inconsistency with the vector is magnified).  tol_dt = the residual
-// tolerance times dt (KEP_TOL * dt by default).  LEARNED selects the MLP
-// starter (weights `mlp`), with the classic starter outside the network's
-// training box and as the restart when the Newton passes from the learned
-// guess do not converge; otherwise `starter` picks the classic or the series
-// starter.
+// The invariants of one drift that the starters and the solver read.
+struct DriftInvariants {
+    double r0, u, mu_r, alpha, T;   // |r|, r.v, mu/|r|, 2 mu/|r| - v^2, dt/|r|
+    float tau2;                     // (dt / dynamical time)^2, FP32
+};
+
+__device__ __forceinline__ DriftInvariants drift_invariants(double rx, double ry, double rz, double vx, double vy,
+                                                            double vz, double r2, double rinv, double dt, double mu)
+{
+    DriftInvariants q;
+    q.r0 = r2 * rinv;
+    const double v2 = fma(vx, vx, fma(vy, vy, vz * vz));
+    q.u = fma(rx, vx, fma(ry, vy, rz * vz));
+    q.mu_r = mu * rinv;
+    q.alpha = fma(2.0, q.mu_r, -v2);
+    q.T = dt * rinv;
+    q.tau2 = tau2_f32(q.T, q.mu_r);
+    return q;
+}
+
+// Drifts (r, v) by dt about a central mass mu, given the drift's invariants
+// q.  r2 = |r|^2 and rinv = 1/|r| come in for the state and go out for the
+// new position, both taken from the new position vector itself (its length
+// enters the energy alpha = 2 mu / r0 - v^2 of the next drift, where near
+// pericentre of an eccentric orbit any inconsistency with the vector is
+// magnified).  tol_dt = the residual tolerance times dt (KEP_TOL * dt by
+// default).  LEARNED: `guess` is the network's starting s (non-positive
+// outside its training box, where the classic starter runs; the classic
+// starter is also the restart when the Newton passes from the network's
+// guess do not converge); otherwise `starter` picks the classic or the
+// series starter.
 template <bool LEARNED>
 __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, double& rz, double& vx, double& vy, double& vz,
-                                                   double& r2_io, double& rinv_io, double dt, double mu, int starter,
-                                                   const MlpDev* mlp, double tol_dt)
+                                                   double& r2_io, double& rinv_io, const DriftInvariants& q, double dt,
+                                                   double mu, int starter, double guess, double tol_dt)
 {
     const double rinv = rinv_io;
-    const double r0 = r2_io * rinv;
-    double v2 = fma(vx, vx, fma(vy, vy, vz * vz));
-    double u = fma(rx, vx, fma(ry, vy, rz * vz));
-    double mu_r = mu * rinv;
-    double alpha = fma(2.0, mu_r, -v2);
+    const double r0 = q.r0, u = q.u, mu_r = q.mu_r, alpha = q.alpha, T = q.T;
     DriftResult res;
     res.flags = __double_as_longlong(alpha) <= 0 ? 0x08 : 0;   // alpha <= 0 (or negative NaN), integer pipe
     res.evals = 0;
 
-    const double T = dt * rinv;
-    const float tau2 = tau2_f32(T, mu_r);                 // (dt / dynamical time)^2
     double s;
     [[maybe_unused]] bool from_mlp = false;
     if constexpr (LEARNED) {
-        s = starter_learned(mlp, T, rinv, tau2, u, mu_r, alpha);
-        from_mlp = s > 0;
-        if (!from_mlp) s = starter_classic(dt, r0, rinv, mu, alpha, u);
+        from_mlp = guess > 0;
+        s = from_mlp ? guess : starter_classic(dt, r0, rinv, mu, alpha, u);
     } else if (starter == STARTER_CLASSIC) {
         s = starter_classic(dt, r0, rinv, mu, alpha, u);
     } else {
-        if (tau2 < SERIES_TAU2_MAX) s = starter_series(T, rinv, alpha, u, mu_r);
+        if (q.tau2 < SERIES_TAU2_MAX) s = starter_series(T, rinv, alpha, u, mu_r);
         else if (alpha > 0) s = starter_fp32_kepler(dt, r0, mu, alpha, u);
         else s = starter_classic(dt, r0, rinv, mu, alpha, u);
     }
@@ -558,6 +572,19 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
     r2_io = nr2;
     rinv_io = nrinv;
     return res;
+}
+
+// The same drift for a single particle: invariants and, LEARNED, the scalar
+// network (weights `mlp`) evaluated here.
+template <bool LEARNED>
+__device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, double& rz, double& vx, double& vy, double& vz,
+                                                   double& r2_io, double& rinv_io, double dt, double mu, int starter,
+                                                   const MlpDev* mlp, double tol_dt)
+{
+    const DriftInvariants q = drift_invariants(rx, ry, rz, vx, vy, vz, r2_io, rinv_io, dt, mu);
+    double guess = -1.0;
+    if constexpr (LEARNED) guess = starter_learned(mlp, q.T, rinv_io, q.tau2, q.u, q.mu_r, q.alpha);
+    return kepler_drift<LEARNED>(rx, ry, rz, vx, vy, vz, r2_io, rinv_io, q, dt, mu, starter, guess, tol_dt);
 }
 
 }  // namespace glisser

@@ -4,8 +4,10 @@
 //
 // Training kernel layout: one CTA of 128 threads takes a tile of 128
 // samples, one per thread.  Each thread runs the forward pass of its sample
-// in exactly the order of mlp_forward (so the trained network is the one the
-// drift evaluates), keeps the pre-activations of the second layer in
+// in the order of mlp_forward, the hidden activations rounded to the BF16
+// hi + lo pair the tensor-core layer reads (gradients straight through the
+// rounding), so the trained network is the one the drift evaluates; it
+// keeps the pre-activations of the second layer in
 // registers, and runs the backward pass to the per-sample deltas, which it
 // writes to shared-memory tiles (rows padded to 33 floats: the row-per-thread
 // writes and the column reads are both bank-conflict free).  The weight
@@ -170,7 +172,7 @@ __global__ void __launch_bounds__(TT) grad_kernel(const float* __restrict__ para
         z = fmaf(W1[4 * j], x0, z);
         z = fmaf(W1[4 * j + 1], x1, z);
         z = fmaf(W1[4 * j + 2], x2, z);
-        h1[j] = z * mlp_sigmoid(z);
+        h1[j] = bf16_split_sum(z * mlp_sigmoid(z));   // as the hidden layer reads it; straight-through below
     }
     float a2[MLP_H];
     float y = B3[0];
@@ -283,22 +285,30 @@ __global__ void adam_kernel(float* params, float* m, float* v, const float* __re
     params[p] -= a.lr * (mm / a.bc1) / (sqrtf(vv / a.bc2) + a.eps);
 }
 
-// The drift's inference routine over a feature list (NaN outside the box).
-__global__ void predict_kernel(const MlpDev* __restrict__ w, const float* __restrict__ feat, uint32_t n, float* y)
+// The time-block kernels' inference (the warp's tensor cores,
+// mlp_forward_warp) over a feature list (NaN outside the box).  Every lane
+// runs the network, lanes past n on zero inputs.
+__global__ void __launch_bounds__(128) predict_kernel(const MlpDev* __restrict__ w, const float* __restrict__ feat,
+                                                      uint32_t n, float* y)
 {
+    __shared__ __align__(16) uint32_t rows[128 / 32][MLP_WARP_WORDS];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float f0 = feat[3 * (size_t)i], f1 = feat[3 * (size_t)i + 1], f2 = feat[3 * (size_t)i + 2];
     const MlpNorm& nm = w->norm;
-    if (!(f0 >= nm.x_lo[0] && f0 <= nm.x_hi[0] && f1 >= nm.x_lo[1] && f1 <= nm.x_hi[1] && f2 >= nm.x_lo[2] &&
-          f2 <= nm.x_hi[2])) {
-        y[i] = __int_as_float(0x7fc00000);
-        return;
+    float x0 = 0.0f, x1 = 0.0f, x2 = 0.0f;
+    bool in_box = false;
+    if (i < n) {
+        const float f0 = feat[3 * (size_t)i], f1 = feat[3 * (size_t)i + 1], f2 = feat[3 * (size_t)i + 2];
+        in_box = f0 >= nm.x_lo[0] && f0 <= nm.x_hi[0] && f1 >= nm.x_lo[1] && f1 <= nm.x_hi[1] && f2 >= nm.x_lo[2] &&
+                 f2 <= nm.x_hi[2];
+        if (in_box) {
+            x0 = (f0 - nm.in_mean[0]) * nm.in_scale[0];
+            x1 = (f1 - nm.in_mean[1]) * nm.in_scale[1];
+            x2 = (f2 - nm.in_mean[2]) * nm.in_scale[2];
+        }
     }
-    const float x0 = (f0 - nm.in_mean[0]) * nm.in_scale[0];
-    const float x1 = (f1 - nm.in_mean[1]) * nm.in_scale[1];
-    const float x2 = (f2 - nm.in_mean[2]) * nm.in_scale[2];
-    y[i] = fmaf(nm.out_scale, mlp_forward(w, x0, x1, x2), nm.out_mean);
+    __syncwarp();
+    const float out = mlp_forward_warp(w, rows[threadIdx.x >> 5], x0, x1, x2);
+    if (i < n) y[i] = in_box ? fmaf(nm.out_scale, out, nm.out_mean) : __int_as_float(0x7fc00000);
 }
 
 // One Kepler drift per state with the time-block kernel's drift routine.
@@ -349,6 +359,9 @@ MlpDev make_dev(const float* params, const MlpNorm& norm)
         for (int k = 0; k < MLP_IN; k++) d.w1[j][k] = bf16_round_host(params[MLP_OFF_W1 + j * MLP_IN + k]);
         d.b1[j] = params[MLP_OFF_B1 + j];
         for (int k = 0; k < MLP_H; k++) d.w2[j][k] = bf16_round_host(params[MLP_OFF_W2 + j * MLP_H + k]);
+        for (int q = 0; q < MLP_H / 2; q++)
+            d.w2p[j][q] = (bf16_bits_round(params[MLP_OFF_W2 + j * MLP_H + 2 * q]) >> 16) |
+                          (bf16_bits_round(params[MLP_OFF_W2 + j * MLP_H + 2 * q + 1]) & 0xFFFF0000u);
         d.b2[j] = params[MLP_OFF_B2 + j];
         d.w3[j] = bf16_round_host(params[MLP_OFF_W3 + j]);
     }

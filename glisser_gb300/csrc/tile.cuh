@@ -150,6 +150,10 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
         if (nchunks > 1) { issue_chunk(p, log, stage + bufstride, &sh.bar[1], 1, rec); inflight1 = true; }
     }
 
+    // the learned starter's per-warp activation rows (a placeholder otherwise)
+    __shared__ __align__(16) uint32_t mlp_buf[LEARNED ? CTA / 32 : 1][LEARNED ? MLP_WARP_WORDS : 4];
+    [[maybe_unused]] uint32_t* mlp_rows = mlp_buf[LEARNED ? (tid >> 5) : 0];
+
     double rx[PPT], ry[PPT], rz[PPT], vx[PPT], vy[PPT], vz[PPT], ax[PPT], ay[PPT], az[PPT], r2[PPT], rinv[PPT];
     uint16_t flags[PPT], flags0[PPT];
     uint32_t dti[PPT];
@@ -217,9 +221,25 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
             const ff* L = L0 + (size_t)s * rec;
 #pragma unroll
             for (int k = 0; k < PPT; k++) {
+                DriftInvariants q;
+                double guess = -1.0;
+                if constexpr (LEARNED) {
+                    // every lane, flagged or not: the network runs on the
+                    // warp's tensor cores (zero inputs for a lane without a drift)
+                    q = drift_invariants(rx[k], ry[k], rz[k], vx[k], vy[k], vz[k], r2[k], rinv[k], p.dt, mu);
+                    float x0 = 0.0f, x1 = 0.0f, x2 = 0.0f;
+                    const bool in_box =
+                        flags[k] == 0 && mlp_inputs(p.mlp, q.tau2, q.u, rinv[k], q.mu_r, q.alpha, x0, x1, x2);
+                    if (!in_box) x0 = x1 = x2 = 0.0f;
+                    __syncwarp();
+                    const float y = mlp_forward_warp(p.mlp, mlp_rows, x0, x1, x2);
+                    if (in_box) guess = learned_guess(p.mlp, q.T, q.tau2, y);
+                }
                 if (flags[k] != 0) continue;
-                DriftResult d = kepler_drift<LEARNED>(rx[k], ry[k], rz[k], vx[k], vy[k], vz[k], r2[k], rinv[k], p.dt,
-                                                       mu, p.starter, p.mlp, p.tol_dt);
+                if constexpr (!LEARNED)
+                    q = drift_invariants(rx[k], ry[k], rz[k], vx[k], vy[k], vz[k], r2[k], rinv[k], p.dt, mu);
+                DriftResult d = kepler_drift<LEARNED>(rx[k], ry[k], rz[k], vx[k], vy[k], vz[k], r2[k], rinv[k], q,
+                                                       p.dt, mu, p.starter, guess, p.tol_dt);
                 uint16_t fl = d.flags;
                 evals += d.evals;
                 const ff fx = ff_split(rx[k]), fy = ff_split(ry[k]), fz = ff_split(rz[k]);

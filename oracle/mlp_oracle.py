@@ -36,6 +36,16 @@ def bf16(x):
     return u.astype(np.uint32).view(np.float32)
 
 
+def bf16_split(h):
+    """Hidden activations as the hidden layer reads them: the float32 value
+    h rounded to BF16 (hi) plus the remainder rounded to BF16 (lo), float64
+    (~16 significant bits; mlp.cuh bf16_split_sum)."""
+    h32 = np.asarray(h, np.float32)
+    hi = bf16(h32)
+    lo = bf16((h32 - hi).astype(np.float32))
+    return hi.astype(np.float64) + lo.astype(np.float64)
+
+
 def effective(params):
     """The parameter values the kernels compute with: BF16 weights, FP32 biases (float64 arrays)."""
     p = np.asarray(params, np.float32).copy()
@@ -58,12 +68,16 @@ def normalise(feat, norm):
     return (f - np.asarray(norm["in_mean"], np.float64)) * np.asarray(norm["in_scale"], np.float64)
 
 
-def forward(p, x):
+def forward(p, x, split=True):
     """Network output (normalised units) for normalised inputs x [n, 3];
-    p = effective parameters (float64).  Returns (out, cache)."""
+    p = effective parameters (float64).  split: the hidden activations as
+    the kernels read them (bf16_split); False gives the smooth network, whose
+    chain rule the finite-difference check pins.  Returns (out, cache)."""
     W1, b1, W2, b2, w3, b3 = _split(p)
     a1 = x @ W1.T + b1
     h1 = a1 * _sig(a1)
+    if split:
+        h1 = bf16_split(h1)
     a2 = h1 @ W2.T + b2
     h2 = a2 * _sig(a2)
     out = h2 @ w3 + b3
@@ -79,13 +93,15 @@ def predict(params, norm, feat):
     return np.where(inside, y, np.nan)
 
 
-def loss_and_grad(params, norm, feat, target, p_eff=None):
+def loss_and_grad(params, norm, feat, target, p_eff=None, split=True):
     """Mean squared error of the normalised output and its gradient with
-    respect to the (effective) parameters, float64."""
+    respect to the (effective) parameters, float64; with split, the
+    gradient passes straight through the activations' BF16 rounding, as in
+    the training kernel."""
     p = effective(params) if p_eff is None else p_eff
     x = normalise(feat, norm)
     tn = (np.asarray(target, np.float64) - float(norm["out_mean"])) / float(norm["out_scale"])
-    out, (x, a1, h1, a2, h2) = forward(p, x)
+    out, (x, a1, h1, a2, h2) = forward(p, x, split)
     n = len(tn)
     e = out - tn
     loss = np.mean(e * e)
@@ -105,10 +121,10 @@ def loss_and_grad(params, norm, feat, target, p_eff=None):
     return loss, g
 
 
-def loss_only(p_eff, norm, feat, target):
+def loss_only(p_eff, norm, feat, target, split=True):
     x = normalise(feat, norm)
     tn = (np.asarray(target, np.float64) - float(norm["out_mean"])) / float(norm["out_scale"])
-    out, _ = forward(p_eff, x)
+    out, _ = forward(p_eff, x, split)
     return np.mean((out - tn) ** 2)
 
 

@@ -134,8 +134,14 @@ def test_inference_matches_oracle(trained):
     y_ref = M.predict(tr.params, tr.norm, feat.astype(np.float64))
     ok = np.isfinite(y_ref)
     assert np.array_equal(np.isfinite(y_gpu), ok)
+    # the GPU runs the time-block kernels' inference: the hidden layer on the
+    # tensor cores.  The FP32 activations and the oracle's float64 ones can
+    # round to different BF16 hi/lo pairs at a rounding boundary (2^-17 of an
+    # activation), hence the looser bound on the few largest differences.
     scale = float(tr.norm["out_scale"])
-    assert np.max(np.abs(y_gpu[ok] - y_ref[ok])) < 3e-5 * scale + 1e-6
+    d = np.abs(y_gpu[ok] - y_ref[ok])
+    assert np.quantile(d, 0.999) < 3e-5 * scale + 1e-6
+    assert d.max() < 3e-4 * scale + 1e-6
 
 
 def test_learned_starter_saves_newton_passes(trained):

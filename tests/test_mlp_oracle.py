@@ -31,10 +31,13 @@ def _case(seed, n=40):
 
 
 def test_gradient_matches_finite_differences():
+    """The chain rule on the smooth network (no activation rounding, which
+    the kernels' gradient passes straight through)."""
     p, norm, feat, target = _case(1)
     pe = M.effective(p)
-    loss, g = M.loss_and_grad(p, norm, feat, target)
-    assert np.isclose(loss, M.loss_only(pe, norm, feat, target), rtol=1e-14)
+    loss, g = M.loss_and_grad(p, norm, feat, target, split=False)
+    assert np.isclose(loss, M.loss_only(pe, norm, feat, target, split=False), rtol=1e-14)
+    assert np.isclose(M.loss_and_grad(p, norm, feat, target)[0], M.loss_only(pe, norm, feat, target), rtol=1e-14)
     rng = np.random.default_rng(7)
     idx = np.concatenate([rng.choice(np.arange(a, b), 6, replace=False) for a, b in
                           ((M.OFF_W1, M.OFF_B1), (M.OFF_B1, M.OFF_W2), (M.OFF_W2, M.OFF_B2),
@@ -42,9 +45,9 @@ def test_gradient_matches_finite_differences():
     for i in idx:
         h = 1e-6 * max(1.0, abs(pe[i]))
         q = pe.copy(); q[i] += h
-        lp = M.loss_only(q, norm, feat, target)
+        lp = M.loss_only(q, norm, feat, target, split=False)
         q[i] -= 2 * h
-        lm = M.loss_only(q, norm, feat, target)
+        lm = M.loss_only(q, norm, feat, target, split=False)
         fd = (lp - lm) / (2 * h)
         assert abs(fd - g[i]) <= 1e-6 * max(abs(g).max(), 1e-12), (i, fd, g[i])
 
@@ -57,3 +60,15 @@ def test_predict_box_and_scaling():
     assert np.all(np.isnan(y[~inside])) and np.all(np.isfinite(y[inside]))
     out, _ = M.forward(M.effective(p), M.normalise(feat, norm))
     assert np.allclose(y[inside], norm["out_mean"] + norm["out_scale"] * out[inside], rtol=0, atol=1e-15)
+
+
+def test_activation_split_keeps_sixteen_bits():
+    rng = np.random.default_rng(3)
+    h = rng.normal(0, 2, 10000).astype(np.float32)
+    got = M.bf16_split(h)
+    rel = np.abs(got - h.astype(np.float64)) / np.abs(h.astype(np.float64))
+    assert rel.max() <= 2.0 ** -16
+    hi = M.bf16(h)
+    assert np.all((hi.view(np.uint32) & 0xFFFF) == 0)
+    lo = (got - hi.astype(np.float64)).astype(np.float32)
+    assert np.all((lo.view(np.uint32) & 0xFFFF) == 0)   # the remainder is a BF16 value too
