@@ -18,12 +18,20 @@ using namespace tile;
 #define GLISSER_TB_MIN_BLOCKS 10
 #endif
 
-// The learned-starter kernel carries the MLP's 32 hidden activations on top
-// of the drift's registers.  A bound of 7 CTAs per SM (ptxas still picks 128
-// registers, spilling 96 bytes) measured 1.6 % faster than 8 (128, 136
-// bytes spilled) and 8 % faster than 6 or 9.
+// The learned-starter kernel carries the network's layer-1 activations and
+// the hidden layer's accumulators on top of the drift's registers.  A bound
+// of 7 CTAs per SM (ptxas picks 128 registers, spilling 72 bytes) measured
+// within 1 % of 5, 6 and 8.
 #ifndef GLISSER_TB_MIN_BLOCKS_LEARNED
 #define GLISSER_TB_MIN_BLOCKS_LEARNED 7
+#endif
+
+// Particles per thread of the plain-starter kernel (a build-time tuning
+// knob; the learned kernel keeps one).  Two (118 registers, 8 CTAs per SM)
+// measured 14 % slower on the plain-giants workload and 36 % on the
+// scattered disk, where the warp-uniform Stumpff tiers diverge more often.
+#ifndef GLISSER_TB_PPT
+#define GLISSER_TB_PPT 1
 #endif
 
 template <int NP, bool LEARNED>
@@ -37,8 +45,10 @@ __global__ void __launch_bounds__(BLOCK_THREADS, LEARNED ? GLISSER_TB_MIN_BLOCKS
     init_barriers(sh);
     __syncthreads();
     uint32_t phase[2] = { 0, 0 };
-    const uint32_t first = blockIdx.x * BLOCK_THREADS;
-    run_tile<NP, BLOCK_THREADS, 1, LEARNED>(p, log, first, min((uint32_t)BLOCK_THREADS, n - first), stage, sh, phase);
+    constexpr int PPT = LEARNED ? 1 : GLISSER_TB_PPT;
+    const uint32_t first = blockIdx.x * (uint32_t)(BLOCK_THREADS * PPT);
+    run_tile<NP, BLOCK_THREADS, PPT, LEARNED>(p, log, first, min((uint32_t)(BLOCK_THREADS * PPT), n - first), stage,
+                                              sh, phase);
 }
 
 template <int NP, bool LEARNED>
@@ -47,7 +57,8 @@ cudaError_t launch_np(const Common& p, const glisser_planet_block* pl, uint32_t 
     auto kern = timeblock_kernel<NP, LEARNED>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    uint32_t grid = (n + BLOCK_THREADS - 1) / BLOCK_THREADS;
+    const uint32_t per_cta = (uint32_t)BLOCK_THREADS * (LEARNED ? 1u : (uint32_t)GLISSER_TB_PPT);
+    const uint32_t grid = (n + per_cta - 1) / per_cta;
     kern<<<grid, BLOCK_THREADS, smem, stream>>>(p, pl->log, pl->m, pl->rh, pl->id, n);
     return cudaGetLastError();
 }
