@@ -33,7 +33,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s on 1 GB300, learned+batched vs plain, at <=1e-10 rel pos err"
 UNIT = "particle-steps/s"
-DRAM_BYTES_PER_PARTICLE_BLOCK = 76.6
+DRAM_BYTES_PER_PARTICLE_BLOCK = 80.4
 KEPLER_TOL_SCATTERED = 1e-14     # the scattered-disk workload's Newton tolerance
 # FP64 thread-instructions per particle-step of timeblock_kernel<4> (series
 # starter) counted by ncu (smsp__sass_thread_inst_executed_op_d{add,fma,mul}),
@@ -812,7 +812,7 @@ def main():
     F = alg_flops_per_particle_step(n_planets)
     achieved_tf = sum(p * F for p in psteps) / (sum(kernel_ms) * 1e-3) / 1e12
     value_kernel = sum(psteps) / (sum(kernel_ms) * 1e-3)
-    # DRAM bytes per launch: ncu measured 76.6 B per particle per block
+    # DRAM bytes per launch: ncu measured 80.4 B per particle per block
     # (dram__bytes_read + write on a 131,072-particle launch, T = 2048), scaled
     # by the particles a launch processes
     traffic = DRAM_BYTES_PER_PARTICLE_BLOCK * (sum(psteps) / len(psteps)) / args.tbsize
