@@ -155,8 +155,11 @@ def test_learned_starter_saves_newton_passes(trained):
     print("mean Stumpff evaluations per drift:", ev)
     assert ev["learned"] < ev["classic"] - 0.5
     # the series starter (orders 2-4 in float-float) is accepted on the first
-    # FP64 evaluation almost everywhere
+    # FP64 evaluation almost everywhere, and so is the network's guess, by
+    # predicted acceptance (its reverted correction provably lands within
+    # the tolerance)
     assert ev["series"] < 1.05
+    assert ev["learned"] < 1.1
     for k in ("learned", "series"):
         assert np.array_equal(out[k][3], out["classic"][3])
         rr = np.linalg.norm(out[k][0] - out["classic"][0], axis=1) / np.linalg.norm(out["classic"][0], axis=1)
