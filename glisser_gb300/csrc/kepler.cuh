@@ -6,8 +6,10 @@
 // spec is kepu, src/wh.cpp:131-420, itself SWIFT's drift_kepu*), then applies
 // the f and g functions (src/wh.cpp:843-851).
 //
-// The arithmetic is FP64 throughout.  GB300 issues FP64 at a small fraction
-// of its FP32 rate, so the solver is written to minimise FP64 instructions:
+// The state, the Kepler residual and the solution are FP64.  GB300 issues
+// FP64 at a small fraction of its FP32 rate, so the solver is written to
+// minimise FP64 instructions, moving to the FP32 and integer pipes what
+// provably does not need FP64:
 //  * one FP64 reciprocal per Newton pass: the quartic correction is the
 //    series reversion  ds = -h - A h^2 + (B - 2A^2) h^3  (h = f/f',
 //    A = f''/2f', B = f'''/6f'), which has the same fourth-order
@@ -30,6 +32,9 @@
 //    Stumpff evaluation per drift;
 //  * threshold tests on non-negative values compare the IEEE bit patterns as
 //    integers (same answer, including NaN, but on the integer pipe);
+//  * in the FP64-bound kernels the accepted correction's fold and the
+//    float-float sums return to FP64 by integer additions to the bit
+//    patterns (f64_add_tiny, ff_to_f64 in fastmath.cuh);
 //  * the Stumpff series is evaluated by Horner in x = alpha s^2; arguments
 //    with |x| >= 0.1 are quartered and rebuilt with the double-angle
 //    identities (c0,c1,c2,c3 as in Danby eq. 6.9.15).
