@@ -76,7 +76,10 @@ __device__ __forceinline__ float bf16_split_sum(float h)
 // SiLU and its derivative; the same routine in training and inference.
 __device__ __forceinline__ float mlp_sigmoid(float a) { return __fdividef(1.0f, 1.0f + __expf(-a)); }
 
-// Network output (normalised units) for normalised inputs x0..x2.  Weight
+// Network output (normalised units) for normalised inputs x0..x2, per
+// thread in FP32 (the single-drift entry point kepler_drift(..., mlp, ...)
+// and the tests; the time-block kernels use mlp_forward_warp, the same
+// values on the tensor cores up to the order of the FP32 sums).  Weight
 // rows are read with 16-byte loads; every thread of a warp reads the same
 // address, so each load is one broadcast transaction.
 __device__ __forceinline__ float mlp_forward(const MlpDev* __restrict__ w, float x0, float x1, float x2)
