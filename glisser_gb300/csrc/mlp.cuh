@@ -15,15 +15,15 @@
 // passes it takes.
 //
 // The arithmetic is BF16 in, FP32 accumulate: weights hold BF16 values
-// (rounded from the FP32 master copy); the hidden layer's 32 x 32 product
-// reads its inputs as the sum of two BF16 values (hi = the activation
-// rounded, lo = the remainder rounded: ~16 significant bits) and accumulates
-// in FP32.  In the time-block kernels that product runs on the tensor cores,
-// one warp's 32 particles at a time (mlp_forward_warp: mma.sync m16n8k16
-// BF16 -> FP32, activations staged through shared memory by ldmatrix); the
-// training kernels and the scalar routine (mlp_forward) compute the same
-// values with FP32 FMAs, so the network is trained on the arithmetic it is
-// used with (up to the order of the FP32 sums).
+// (rounded from the FP32 master copy); both layers' products read their
+// inputs (the normalised features, the hidden activations) as the sum of
+// two BF16 values (hi = the value rounded, lo = the remainder rounded: ~16
+// significant bits) and accumulate in FP32.  In the time-block kernels both
+// products run on the tensor cores, one warp's 32 particles at a time
+// (mlp_forward_warp: mma.sync m16n8k16 BF16 -> FP32); the training kernels
+// and the scalar routine (mlp_forward) compute the same values with FP32
+// FMAs, so the network is trained on the arithmetic it is used with (up to
+// the order of the FP32 sums).
 #pragma once
 #include <cuda_bf16.h>
 #include <cstdint>
@@ -56,6 +56,7 @@ struct __align__(16) MlpDev {
     float b1[MLP_H];
     float w2[MLP_H][MLP_H];          // [out][in]
     uint32_t w2p[MLP_H][MLP_H / 2];  // the same as BF16 pairs (in 2q low half, 2q+1 high): the MMA's B operand
+    uint32_t w1p[MLP_H][4];          // W1 as the layer-1 MMA's B pairs: (w0, w1), (w2, w0), (w1, w2), 0
     float b2[MLP_H];
     float w3[MLP_H];
     float b3;
@@ -84,6 +85,9 @@ __device__ __forceinline__ float mlp_sigmoid(float a) { return __fdividef(1.0f, 
 // address, so each load is one broadcast transaction.
 __device__ __forceinline__ float mlp_forward(const MlpDev* __restrict__ w, float x0, float x1, float x2)
 {
+    x0 = bf16_split_sum(x0);
+    x1 = bf16_split_sum(x1);
+    x2 = bf16_split_sum(x2);
     float h1[MLP_H];
 #pragma unroll
     for (int j = 0; j < MLP_H; j++) {
@@ -162,50 +166,73 @@ __device__ __forceinline__ double starter_learned(const MlpDev* __restrict__ w, 
 // ---------------------------------------------------------------------------
 // The network on the tensor cores, one warp's 32 particles at a time.
 //
-// The hidden layer is H2 = H1 W2^T for H1 [32 particles x 32 units]: two
-// m16 row tiles (lanes 0-15, 16-31) by four n8 column tiles by two k16
-// steps of mma.sync m16n8k16 (BF16 in, FP32 accumulate), each step once
-// with the activations' hi parts and once with their lo parts.  Each lane
-// writes its particle's 16 activations of a k-step into its row of a
-// per-warp shared buffer (hi pairs in words 0-7, lo pairs in 8-15, rows
-// padded to 20 words so that each 8-row ldmatrix phase meets 32 distinct
-// banks); ldmatrix.x4 returns them in the A-fragment layout.  W2 comes from
-// the BF16 pairs in MlpDev (row n = output unit: the "col" B operand).  The
-// accumulators start at the bias; SiLU and the w3 products are applied to
-// each lane's fragment, summed over the four lanes of a row group by two
-// shuffles and handed to the lane that owns the row.
-constexpr int MLP_ROW_WORDS = 20;
-constexpr int MLP_WARP_WORDS = 32 * MLP_ROW_WORDS;   // uint32 words of shared memory per warp
-
+// Both layers run as mma.sync m16n8k16 (BF16 in, FP32 accumulate) over the
+// warp's 32 particles: two m16 row tiles (lanes 0-15, 16-31) by four n8
+// column tiles (the 32 hidden units).
+//   Layer 1: A = the inputs as BF16 pairs, row p = (x0 hi, x1 hi, x2 hi,
+//   x0 lo, x1 lo, x2 lo, 0, ...) of lane p's particle, gathered by shuffles
+//   into the fragment layout; B = W1 with its three columns written twice
+//   (k = 0-2 and 3-5) as packed BF16 pairs (MlpDev::w1p); the accumulators
+//   start at the bias.  One k-step: 8 MMAs.
+//   Layer 2: the layer-1 accumulators of column tiles 2ks and 2ks + 1 are,
+//   after SiLU, exactly the A fragment of k-step ks (the m16n8 C layout of
+//   two adjacent tiles is the m16k16 A layout), so each activation is split
+//   into BF16 hi and lo in registers and used in place: 2 k-steps x 2
+//   (hi, lo) x 8 tiles = 32 MMAs, W2 as packed BF16 pairs (MlpDev::w2p).
+// SiLU and the w3 products are applied to each lane's layer-2 fragment,
+// summed over the four lanes of a row group by two shuffles and handed to
+// the lane that owns the row.
 __device__ __forceinline__ uint32_t bf16x2_bits(float lo, float hi)
 {
     const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);   // .x (low half) = lo
     return *reinterpret_cast<const uint32_t*>(&v);
 }
 
-__device__ __forceinline__ void ldmatrix_x4(uint32_t (&r)[4], uint32_t saddr)
-{
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];\n"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(saddr));
-}
-
-__device__ __forceinline__ void mma_bf16_m16n8k16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
+__device__ __forceinline__ void mma_bf16_m16n8k16(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                                  uint32_t b0, uint32_t b1)
 {
     asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, "
                  "{%8, %9}, {%0, %1, %2, %3};\n"
                  : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+                 : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
 // Network output (normalised units) of every lane's inputs.  All 32 lanes
-// of the warp must call it together (converged); `rows` is the warp's
-// MLP_WARP_WORDS-word shared buffer.
-__device__ __forceinline__ float mlp_forward_warp(const MlpDev* __restrict__ w, uint32_t* rows, float x0, float x1,
-                                                  float x2)
+// of the warp must call it together (converged).
+__device__ __forceinline__ float mlp_forward_warp(const MlpDev* __restrict__ w, float x0, float x1, float x2)
 {
     const unsigned lane = threadIdx.x & 31u;
     const unsigned g = lane >> 2, t = lane & 3u;
+    // this lane's inputs as BF16 pairs (k = 0,1), (2,3), (4,5)
+    const float x0h = bf16_round(x0), x1h = bf16_round(x1), x2h = bf16_round(x2);
+    const uint32_t p0 = bf16x2_bits(x0h, x1h), p1 = bf16x2_bits(x2h, x0 - x0h), p2 = bf16x2_bits(x1 - x1h, x2 - x2h);
+    // layer-1 A fragments: lane (g, t) holds pair t of rows g and g + 8
+    uint32_t a1[2][2];
+#pragma unroll
+    for (int mt = 0; mt < 2; mt++) {
+#pragma unroll
+        for (int hf = 0; hf < 2; hf++) {
+            const int src = mt * 16 + hf * 8 + (int)g;
+            const uint32_t q0 = __shfl_sync(0xffffffffu, p0, src), q1 = __shfl_sync(0xffffffffu, p1, src);
+            const uint32_t q2 = __shfl_sync(0xffffffffu, p2, src);
+            a1[mt][hf] = t == 0 ? q0 : (t == 1 ? q1 : (t == 2 ? q2 : 0u));
+        }
+    }
+    float h[2][4][4];
+#pragma unroll
+    for (int nt = 0; nt < 4; nt++) {
+        const float b_lo = __ldg(&w->b1[nt * 8 + 2 * t]), b_hi = __ldg(&w->b1[nt * 8 + 2 * t + 1]);
+        const uint32_t bw = __ldg(&w->w1p[nt * 8 + g][t]);
+#pragma unroll
+        for (int mt = 0; mt < 2; mt++) {
+            h[mt][nt][0] = b_lo;
+            h[mt][nt][1] = b_hi;
+            h[mt][nt][2] = b_lo;
+            h[mt][nt][3] = b_hi;
+            mma_bf16_m16n8k16(h[mt][nt], a1[mt][0], a1[mt][1], 0u, 0u, bw, 0u);
+        }
+    }
+    // layer 2, the bias as the accumulators' start
     float acc[2][4][4];
 #pragma unroll
     for (int nt = 0; nt < 4; nt++) {
@@ -218,56 +245,29 @@ __device__ __forceinline__ float mlp_forward_warp(const MlpDev* __restrict__ w, 
             acc[mt][nt][3] = b_hi;
         }
     }
-    uint32_t* row = rows + lane * MLP_ROW_WORDS;
-    // ldmatrix row address of this lane: matrix (lane / 8) of the x4 load is
-    // (rows +0 / +8) x (columns +0 / +8) of the 16 x 16 A tile
-    const unsigned arow = (lane & 7u) + ((lane >> 3) & 1u) * 8u, acol = (lane >> 4) * 4u;
-    const uint32_t abase = (uint32_t)__cvta_generic_to_shared(rows) + 4u * (arow * MLP_ROW_WORDS + acol);
 #pragma unroll
     for (int ks = 0; ks < 2; ks++) {
-        // layer 1 for units 16 ks .. 16 ks + 15, split into BF16 hi / lo
-        // pairs and stored as four 16-byte words (conflict-free: 8 lanes of
-        // a phase write 8 different 16-byte bank groups)
-        uint32_t hp[8], lp[8];
-#pragma unroll
-        for (int q = 0; q < 8; q++) {
-            float h[2];
-#pragma unroll
-            for (int e = 0; e < 2; e++) {
-                const int j = ks * 16 + 2 * q + e;
-                const float4 r = __ldg(reinterpret_cast<const float4*>(w->w1[j]));
-                float a = __ldg(&w->b1[j]);
-                a = fmaf(r.x, x0, a);
-                a = fmaf(r.y, x1, a);
-                a = fmaf(r.z, x2, a);
-                h[e] = a * mlp_sigmoid(a);
-            }
-            const float h0 = bf16_round(h[0]), h1 = bf16_round(h[1]);
-            hp[q] = bf16x2_bits(h0, h1);
-            lp[q] = bf16x2_bits(h[0] - h0, h[1] - h1);
-        }
-        uint4* row4 = reinterpret_cast<uint4*>(row);
-        row4[0] = make_uint4(hp[0], hp[1], hp[2], hp[3]);
-        row4[1] = make_uint4(hp[4], hp[5], hp[6], hp[7]);
-        row4[2] = make_uint4(lp[0], lp[1], lp[2], lp[3]);
-        row4[3] = make_uint4(lp[4], lp[5], lp[6], lp[7]);
-        __syncwarp();
-        uint32_t a_hi[2][4], a_lo[2][4];
+        uint32_t ahi[2][4], alo[2][4];
 #pragma unroll
         for (int mt = 0; mt < 2; mt++) {
-            const uint32_t at = abase + 4u * (mt * 16u * MLP_ROW_WORDS);
-            ldmatrix_x4(a_hi[mt], at);
-            ldmatrix_x4(a_lo[mt], at + 4u * 8u);
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+                // register r of the A fragment: tile 2ks + (r >> 1), row half (r & 1)
+                const float* c = &h[mt][2 * ks + (r >> 1)][2 * (r & 1)];
+                const float s0 = c[0] * mlp_sigmoid(c[0]), s1 = c[1] * mlp_sigmoid(c[1]);
+                const float s0h = bf16_round(s0), s1h = bf16_round(s1);
+                ahi[mt][r] = bf16x2_bits(s0h, s1h);
+                alo[mt][r] = bf16x2_bits(s0 - s0h, s1 - s1h);
+            }
         }
-        __syncwarp();   // the rows are rewritten by the next k-step
 #pragma unroll
         for (int nt = 0; nt < 4; nt++) {
             const uint32_t b0 = __ldg(&w->w2p[nt * 8 + g][ks * 8 + t]);
             const uint32_t b1 = __ldg(&w->w2p[nt * 8 + g][ks * 8 + t + 4]);
 #pragma unroll
             for (int mt = 0; mt < 2; mt++) {
-                mma_bf16_m16n8k16(acc[mt][nt], a_hi[mt], b0, b1);
-                mma_bf16_m16n8k16(acc[mt][nt], a_lo[mt], b0, b1);
+                mma_bf16_m16n8k16(acc[mt][nt], ahi[mt][0], ahi[mt][1], ahi[mt][2], ahi[mt][3], b0, b1);
+                mma_bf16_m16n8k16(acc[mt][nt], alo[mt][0], alo[mt][1], alo[mt][2], alo[mt][3], b0, b1);
             }
         }
     }

@@ -157,9 +157,10 @@ __global__ void __launch_bounds__(TT) grad_kernel(const float* __restrict__ para
     }
     float x0 = 0, x1 = 0, x2 = 0, tn = 0;
     if (valid) {
-        x0 = (f0 - a.norm.in_mean[0]) * a.norm.in_scale[0];
-        x1 = (f1 - a.norm.in_mean[1]) * a.norm.in_scale[1];
-        x2 = (f2 - a.norm.in_mean[2]) * a.norm.in_scale[2];
+        // the inputs as the first layer reads them (BF16 hi + lo)
+        x0 = bf16_split_sum((f0 - a.norm.in_mean[0]) * a.norm.in_scale[0]);
+        x1 = bf16_split_sum((f1 - a.norm.in_mean[1]) * a.norm.in_scale[1]);
+        x2 = bf16_split_sum((f2 - a.norm.in_mean[2]) * a.norm.in_scale[2]);
         tn = (tg - a.norm.out_mean) / a.norm.out_scale;
     }
 
@@ -291,7 +292,6 @@ __global__ void adam_kernel(float* params, float* m, float* v, const float* __re
 __global__ void __launch_bounds__(128) predict_kernel(const MlpDev* __restrict__ w, const float* __restrict__ feat,
                                                       uint32_t n, float* y)
 {
-    __shared__ __align__(16) uint32_t rows[128 / 32][MLP_WARP_WORDS];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const MlpNorm& nm = w->norm;
     float x0 = 0.0f, x1 = 0.0f, x2 = 0.0f;
@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(128) predict_kernel(const MlpDev* __restrict__
         }
     }
     __syncwarp();
-    const float out = mlp_forward_warp(w, rows[threadIdx.x >> 5], x0, x1, x2);
+    const float out = mlp_forward_warp(w, x0, x1, x2);
     if (i < n) y[i] = in_box ? fmaf(nm.out_scale, out, nm.out_mean) : __int_as_float(0x7fc00000);
 }
 
@@ -357,6 +357,16 @@ MlpDev make_dev(const float* params, const MlpNorm& norm)
     std::memset(&d, 0, sizeof d);
     for (int j = 0; j < MLP_H; j++) {
         for (int k = 0; k < MLP_IN; k++) d.w1[j][k] = bf16_round_host(params[MLP_OFF_W1 + j * MLP_IN + k]);
+        {
+            // the layer-1 MMA's B pairs: W1's columns at k = 0-2 and again at 3-5
+            const uint32_t b0 = bf16_bits_round(params[MLP_OFF_W1 + j * MLP_IN]) >> 16;
+            const uint32_t b1 = bf16_bits_round(params[MLP_OFF_W1 + j * MLP_IN + 1]) >> 16;
+            const uint32_t b2 = bf16_bits_round(params[MLP_OFF_W1 + j * MLP_IN + 2]) >> 16;
+            d.w1p[j][0] = b0 | (b1 << 16);
+            d.w1p[j][1] = b2 | (b0 << 16);
+            d.w1p[j][2] = b1 | (b2 << 16);
+            d.w1p[j][3] = 0u;
+        }
         d.b1[j] = params[MLP_OFF_B1 + j];
         for (int k = 0; k < MLP_H; k++) d.w2[j][k] = bf16_round_host(params[MLP_OFF_W2 + j * MLP_H + k]);
         for (int q = 0; q < MLP_H / 2; q++)

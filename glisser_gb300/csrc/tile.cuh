@@ -150,10 +150,6 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
         if (nchunks > 1) { issue_chunk(p, log, stage + bufstride, &sh.bar[1], 1, rec); inflight1 = true; }
     }
 
-    // the learned starter's per-warp activation rows (a placeholder otherwise)
-    __shared__ __align__(16) uint32_t mlp_buf[LEARNED ? CTA / 32 : 1][LEARNED ? MLP_WARP_WORDS : 4];
-    [[maybe_unused]] uint32_t* mlp_rows = mlp_buf[LEARNED ? (tid >> 5) : 0];
-
     double rx[PPT], ry[PPT], rz[PPT], vx[PPT], vy[PPT], vz[PPT], ax[PPT], ay[PPT], az[PPT], r2[PPT], rinv[PPT];
     uint16_t flags[PPT], flags0[PPT];
     uint32_t dti[PPT];
@@ -232,7 +228,7 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
                         flags[k] == 0 && mlp_inputs(p.mlp, q.tau2, q.u, rinv[k], q.mu_r, q.alpha, x0, x1, x2);
                     if (!in_box) x0 = x1 = x2 = 0.0f;
                     __syncwarp();
-                    const float y = mlp_forward_warp(p.mlp, mlp_rows, x0, x1, x2);
+                    const float y = mlp_forward_warp(p.mlp, x0, x1, x2);
                     if (in_box) guess = learned_guess(p.mlp, q.T, q.tau2, y);
                 }
                 if (flags[k] != 0) continue;

@@ -70,10 +70,13 @@ def normalise(feat, norm):
 
 def forward(p, x, split=True):
     """Network output (normalised units) for normalised inputs x [n, 3];
-    p = effective parameters (float64).  split: the hidden activations as
-    the kernels read them (bf16_split); False gives the smooth network, whose
+    p = effective parameters (float64).  split: the inputs and the hidden
+    activations as the kernels read them (bf16_split); False gives the
+    smooth network, whose
     chain rule the finite-difference check pins.  Returns (out, cache)."""
     W1, b1, W2, b2, w3, b3 = _split(p)
+    if split:
+        x = bf16_split(x)
     a1 = x @ W1.T + b1
     h1 = a1 * _sig(a1)
     if split:
@@ -101,7 +104,7 @@ def loss_and_grad(params, norm, feat, target, p_eff=None, split=True):
     p = effective(params) if p_eff is None else p_eff
     x = normalise(feat, norm)
     tn = (np.asarray(target, np.float64) - float(norm["out_mean"])) / float(norm["out_scale"])
-    out, (x, a1, h1, a2, h2) = forward(p, x, split)
+    out, (x, a1, h1, a2, h2) = forward(p, x, split)      # x: the inputs as the first layer read them
     n = len(tn)
     e = out - tn
     loss = np.mean(e * e)
