@@ -4,9 +4,10 @@
 //
 // Training kernel layout: one CTA of 128 threads takes a tile of 128
 // samples, one per thread.  Each thread runs the forward pass of its sample
-// in the order of mlp_forward, the hidden activations rounded to the BF16
-// hi + lo pair the tensor-core layer reads (gradients straight through the
-// rounding), so the trained network is the one the drift evaluates; it
+// in the order of mlp_forward, the inputs and the hidden activations rounded
+// to the BF16 hi + lo pairs the tensor-core layers read (gradients straight
+// through the rounding), so the trained network is the one the drift
+// evaluates; it
 // keeps the pre-activations of the second layer in
 // registers, and runs the backward pass to the per-sample deltas, which it
 // writes to shared-memory tiles (rows padded to 33 floats: the row-per-thread
