@@ -20,6 +20,8 @@ E_INVALID, E_CONFIG, E_IO, E_CUDA, E_STATE, E_NOMEM, E_EOS, E_RUNTIME, E_TIMEOUT
 STARTER_CLASSIC, STARTER_SERIES, STARTER_LEARNED = 0, 1, 2
 # StepParams.kill_encounters: what a particle ending the block in an encounter keeps
 ENCOUNTERS_KEEP, ENCOUNTERS_KILL, ENCOUNTERS_ROLLBACK = 0, 1, 2
+# StepParams.kick / set_kick: arithmetic of the planet kick and its radius tests
+KICK_FLOAT_FLOAT, KICK_FP64 = 0, 1
 FLAG_ENCOUNTER, FLAG_OUT_OF_BOUNDS, FLAG_KEPLER, FLAG_UNBOUND, FLAG_DEAD = 0x01, 0x02, 0x04, 0x08, 0x80
 
 
@@ -57,7 +59,8 @@ class PlanetBlockDev(C.Structure):
 
 class StepParams(C.Structure):
     _fields_ = [("dt", C.c_double), ("outer_radius", C.c_double), ("starter", C.c_int32),
-                ("kill_encounters", C.c_int32), ("mlp", C.c_void_p), ("kepler_tol", C.c_double)]
+                ("kill_encounters", C.c_int32), ("mlp", C.c_void_p), ("kepler_tol", C.c_double),
+                ("kick", C.c_int32), ("reserved", C.c_int32)]
 
 
 class MlpNorm(C.Structure):
@@ -71,7 +74,7 @@ class MlpNorm(C.Structure):
 class HandoffDev(C.Structure):
     _fields_ = [("count", C.c_void_p), ("index", C.c_void_p), ("id", C.c_void_p), ("flags", C.c_void_p),
                 ("deathtime_index", C.c_void_p), ("capacity", C.c_uint32), ("reserved", C.c_uint32),
-                ("status", C.c_void_p), ("evals", C.c_void_p)]
+                ("status", C.c_void_p), ("evals", C.c_void_p), ("borderline", C.c_void_p), ("learned", C.c_void_p)]
 
 
 _lib = None
@@ -107,6 +110,12 @@ def lib():
             "glisser_set_device_output": ([P, C.c_int], C.c_int),
             "glisser_set_kepler_tolerance": ([P, C.c_double], C.c_int),
             "glisser_ensemble_set_kepler_tolerance": ([P, C.c_double], C.c_int),
+            "glisser_set_kick": ([P, C.c_int], C.c_int),
+            "glisser_ensemble_set_kick": ([P, C.c_int], C.c_int),
+            "glisser_borderline": ([P, C.POINTER(C.c_ulonglong)], C.c_int),
+            "glisser_ensemble_borderline": ([P, C.POINTER(C.c_ulonglong)], C.c_int),
+            "glisser_learned_drifts": ([P, C.POINTER(C.c_ulonglong)], C.c_int),
+            "glisser_ensemble_learned_drifts": ([P, C.POINTER(C.c_ulonglong)], C.c_int),
             "glisser_step_block": ([P, C.POINTER(C.c_int), D, D], C.c_int),
             "glisser_run": ([P, C.c_int], C.c_int),
             "glisser_finish": ([P], C.c_int),
@@ -145,6 +154,10 @@ def lib():
             "glisser_ensemble_step": ([P, D], C.c_int),
             "glisser_ensemble_counts": ([P, C.c_size_t, SZ, SZ], C.c_int),
             "glisser_ensemble_get_particles": ([P, C.c_size_t, D, D, U32, U16, C.c_size_t, SZ], C.c_int),
+            "glisser_ensemble_get_deaths": ([P, C.c_size_t, D, U32, C.c_size_t, SZ], C.c_int),
+            "glisser_ensemble_set_state": ([P, C.c_size_t, D, D], C.c_int),
+            "glisser_ensemble_get_state": ([P, D, D, U16, C.c_size_t, SZ], C.c_int),
+            "glisser_ensemble_stream": ([P, C.POINTER(P)], C.c_int),
             "glisser_ensemble_stats": ([P, C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong),
                                         C.POINTER(C.c_ulonglong)], C.c_int),
             "glisser_ensemble_time": ([P, D], C.c_int),
@@ -155,6 +168,7 @@ def lib():
             "glisser_mlp_log_states": ([P, C.POINTER(ParticlesDev), C.c_size_t, C.c_double, C.c_double, P, SZ],
                                        C.c_int),
             "glisser_mlp_add_samples": ([P, F32, F32, C.c_size_t], C.c_int),
+            "glisser_mlp_set_log_floor": ([P, C.c_double], C.c_int),
             "glisser_mlp_get_samples": ([P, F32, F32, C.c_size_t, C.c_size_t], C.c_int),
             "glisser_mlp_samples": ([P, SZ, C.POINTER(C.c_ulonglong)], C.c_int),
             "glisser_mlp_fit_norm": ([P], C.c_int),
@@ -167,6 +181,7 @@ def lib():
             "glisser_mlp_predict": ([P, F32, C.c_size_t, F32], C.c_int),
             "glisser_mlp_save": ([P, C.c_char_p], C.c_int),
             "glisser_mlp_device_weights": ([P, C.POINTER(P)], C.c_int),
+            "glisser_mlp_pack": ([F32, U32, U32], C.c_int),
             "glisser_kepler_drift_states": ([C.POINTER(ParticlesDev), C.c_size_t, C.c_double, C.c_double, C.c_int,
                                              P, P, P, P], C.c_int),
             "glisser_write_stat": ([P, C.c_char_p], C.c_int),
@@ -349,6 +364,11 @@ class Simulation:
         """Track snapshots built on the device (default) or by the host writer."""
         self._check(lib().glisser_set_device_output(self.h, int(bool(on))))
 
+    def set_kick(self, kick):
+        """KICK_FLOAT_FLOAT (default) or KICK_FP64: arithmetic of the planet
+        kick and its radius tests."""
+        self._check(lib().glisser_set_kick(self.h, kick))
+
     def init(self):
         self._check(lib().glisser_init(self.h))
 
@@ -383,10 +403,14 @@ class Simulation:
         return dict(n=n.value, n_alive=na.value, n_encounter=ne.value)
 
     def stats(self):
-        ps, ev, ln = C.c_ulonglong(), C.c_ulonglong(), C.c_ulonglong()
+        ps, ev, ln, bl = C.c_ulonglong(), C.c_ulonglong(), C.c_ulonglong(), C.c_ulonglong()
         lib().glisser_stats(self.h, C.byref(ps), C.byref(ev))
         lib().glisser_launches(self.h, C.byref(ln))
-        return dict(particle_steps=ps.value, kepler_evals=ev.value, launches=ln.value)
+        lib().glisser_borderline(self.h, C.byref(bl))
+        ld = C.c_ulonglong()
+        lib().glisser_learned_drifts(self.h, C.byref(ld))
+        return dict(particle_steps=ps.value, kepler_evals=ev.value, launches=ln.value, borderline=bl.value,
+                    learned_drifts=ld.value)
 
     def stream(self):
         s = C.c_void_p()
@@ -547,6 +571,10 @@ class Ensemble:
         """Planet WH on the device (default) or on the host; before init."""
         self._check(lib().glisser_ensemble_set_device_planets(self.h, int(bool(on))))
 
+    def set_kick(self, kick):
+        """KICK_FLOAT_FLOAT (default) or KICK_FP64, for every system."""
+        self._check(lib().glisser_ensemble_set_kick(self.h, kick))
+
     def planets(self, s, cap=64):
         """Planets of system s at the particles' time (heliocentric)."""
         m = np.zeros(cap); r = np.zeros((cap, 3)); v = np.zeros((cap, 3))
@@ -575,12 +603,42 @@ class Ensemble:
         got = C.c_size_t()
         self._check(lib().glisser_ensemble_get_particles(self.h, s, _p(r, D), _p(v, D), _p(ids, U32), _p(fl, U16),
                                                          n, C.byref(got)))
-        return dict(r=r, v=v, id=ids, flags=fl)
+        dt = np.zeros(n); dti = np.zeros(n, np.uint32)
+        self._check(lib().glisser_ensemble_get_deaths(self.h, s, _p(dt, D), _p(dti, U32), n, C.byref(got)))
+        return dict(r=r, v=v, id=ids, flags=fl, deathtime=dt, deathtime_index=dti)
+
+    def set_state(self, r, v):
+        """Positions and velocities of every particle of every system ([n, 3],
+        system order) for the next block."""
+        r = np.ascontiguousarray(r, np.float64)
+        v = np.ascontiguousarray(v, np.float64)
+        self._check(lib().glisser_ensemble_set_state(self.h, len(r), _p(r, D), _p(v, D)))
+
+    def get_state(self, r=None, v=None, flags=None):
+        """Every particle's r, v [n, 3] and flags, in system order (into the
+        given arrays when passed)."""
+        n = C.c_size_t()
+        self._check(lib().glisser_ensemble_get_state(self.h, None, None, None, 0, C.byref(n)))
+        k = n.value
+        r = np.zeros((k, 3)) if r is None else r
+        v = np.zeros((k, 3)) if v is None else v
+        flags = np.zeros(k, np.uint16) if flags is None else flags
+        self._check(lib().glisser_ensemble_get_state(self.h, _p(r, D), _p(v, D), _p(flags, U16), k, C.byref(n)))
+        return r, v, flags
+
+    def stream(self):
+        s = C.c_void_p()
+        lib().glisser_ensemble_stream(self.h, C.byref(s))
+        return s.value or 0
 
     def stats(self):
-        ps, ev, ln = C.c_ulonglong(), C.c_ulonglong(), C.c_ulonglong()
+        ps, ev, ln, bl = C.c_ulonglong(), C.c_ulonglong(), C.c_ulonglong(), C.c_ulonglong()
         lib().glisser_ensemble_stats(self.h, C.byref(ps), C.byref(ev), C.byref(ln))
-        return dict(particle_steps=ps.value, kepler_evals=ev.value, launches=ln.value)
+        lib().glisser_ensemble_borderline(self.h, C.byref(bl))
+        ld = C.c_ulonglong()
+        lib().glisser_ensemble_learned_drifts(self.h, C.byref(ld))
+        return dict(particle_steps=ps.value, kepler_evals=ev.value, launches=ln.value, borderline=bl.value,
+                    learned_drifts=ld.value)
 
     @property
     def t(self):

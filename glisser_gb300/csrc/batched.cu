@@ -27,16 +27,21 @@ int launch_batched(const glisser_particles* pa, const BatchSystems& sys, const B
     if (!(sp->kepler_tol == 0 || (sp->kepler_tol >= 1e-16 && sp->kepler_tol <= 1e-8))) return GLISSER_E_INVALID;
     if (sp->kill_encounters < GLISSER_ENCOUNTERS_KEEP || sp->kill_encounters > GLISSER_ENCOUNTERS_ROLLBACK)
         return GLISSER_E_INVALID;
+    if (sp->kick != GLISSER_KICK_FLOAT_FLOAT && sp->kick != GLISSER_KICK_FP64) return GLISSER_E_INVALID;
     if (((uintptr_t)sys.log & 15u) != 0 || (sys.log_stride * sizeof(double)) % 16 != 0) return GLISSER_E_INVALID;
     Common p;
     if (!fill_common(p, pa, sp, ho, npl, len, BATCH_LOG_CHUNK)) return GLISSER_E_INVALID;
     size_t smem = timeblock_smem_bytes(npl, (int)p.chunk);
     cudaError_t e;
-    if (sp->starter == GLISSER_STARTER_LEARNED && p.mlp)
+    const bool learned = sp->starter == GLISSER_STARTER_LEARNED && p.mlp;
+    if (learned && p.kick64)
+        e = launch_batched_learned_kick64(p, sys, items, n_items, queue, npl, shape, smem, stream);
+    else if (learned)
         e = launch_batched_learned(p, sys, items, n_items, queue, npl, shape, smem, stream);
+    else if (p.kick64)
+        e = launch_batched_kick64(p, sys, items, n_items, queue, npl, shape, smem, stream);
     else
-        e = npl == 5 ? launch_batched_np<4, false>(p, sys, items, n_items, queue, shape, smem, stream)
-                     : launch_batched_np<0, false>(p, sys, items, n_items, queue, shape, smem, stream);
+        e = launch_batched_variant<false, false>(p, sys, items, n_items, queue, npl, shape, smem, stream);
     if (e != cudaSuccess) {
         char msg[256];
         snprintf(msg, sizeof msg, "batched launch: %s", cudaGetErrorString(e));

@@ -16,15 +16,15 @@ using namespace tile;
 #define GLISSER_BATCHED_THREADS_PER_SM 512
 #endif
 #ifndef GLISSER_BATCHED_THREADS_PER_SM_LEARNED
-#define GLISSER_BATCHED_THREADS_PER_SM_LEARNED 384
+#define GLISSER_BATCHED_THREADS_PER_SM_LEARNED GLISSER_BATCHED_THREADS_PER_SM
 #endif
 
 // Persistent kernel over (system, tile) work items.  Register budget: 128
-// per thread (512 resident threads per SM), or 168 for the learned starter,
-// whose network inference holds 32 hidden activations (384 threads); left
-// free, the compiler sized some learned instantiations for higher occupancy
-// and spilled inside the step loop.
-template <int NP, int CTA, int PPT, bool LEARNED>
+// per thread (512 resident threads per SM).  The learned starter runs its
+// network only in a warp-uniform branch where the series starter is outside
+// its domain and is held to the same budget (what the network needs beyond
+// it is spilled around that branch).
+template <int NP, int CTA, int PPT, bool LEARNED, bool KICK64>
 __global__ void __launch_bounds__(CTA, (LEARNED ? GLISSER_BATCHED_THREADS_PER_SM_LEARNED
                                                 : GLISSER_BATCHED_THREADS_PER_SM) / CTA)
     batched_kernel(const Common p, BatchSystems sys, const BatchItem* items, const uint32_t* n_items, uint32_t* queue)
@@ -43,19 +43,19 @@ __global__ void __launch_bounds__(CTA, (LEARNED ? GLISSER_BATCHED_THREADS_PER_SM
         load_planet_constants(sh, p.npl, sys.m + (size_t)w.system * p.npl, sys.rh + (size_t)w.system * p.npl,
                               sys.id + (size_t)w.system * p.npl);
         __syncthreads();
-        bool ok = run_tile<NP, CTA, PPT, LEARNED>(p, sys.log + (size_t)w.system * sys.log_stride, w.first, w.count, stage, sh,
-                                         phase);
+        bool ok = run_tile<NP, CTA, PPT, LEARNED, KICK64>(p, sys.log + (size_t)w.system * sys.log_stride, w.first,
+                                                          w.count, stage, sh, phase);
         __syncthreads();   // sh.item / planet constants are rewritten by the next item
         if (!ok) break;
     }
 }
 
-template <int NP, int CTA, int PPT, bool LEARNED>
+template <int NP, int CTA, int PPT, bool LEARNED, bool KICK64>
 cudaError_t launch_batched_t(const Common& p, const BatchSystems& sys, const BatchItem* items,
                              const uint32_t* n_items, uint32_t* queue, uint32_t grid, size_t smem,
                              cudaStream_t stream)
 {
-    auto kern = batched_kernel<NP, CTA, PPT, LEARNED>;
+    auto kern = batched_kernel<NP, CTA, PPT, LEARNED, KICK64>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     if (grid == 0) {
@@ -69,28 +69,47 @@ cudaError_t launch_batched_t(const Common& p, const BatchSystems& sys, const Bat
     return cudaGetLastError();
 }
 
-template <int NP, bool LEARNED>
+template <int NP, bool LEARNED, bool KICK64>
 cudaError_t launch_batched_np(const Common& p, const BatchSystems& sys, const BatchItem* items,
                               const uint32_t* n_items, uint32_t* queue, const BatchShape& shape, size_t smem,
                               cudaStream_t stream)
 {
     const int key = shape.cta * 10 + shape.ppt;
+    const uint32_t g = shape.grid;
     switch (key) {
-    case 641: return launch_batched_t<NP, 64, 1, LEARNED>(p, sys, items, n_items, queue, shape.grid, smem, stream);
-    case 642: return launch_batched_t<NP, 64, 2, LEARNED>(p, sys, items, n_items, queue, shape.grid, smem, stream);
-    case 1281: return launch_batched_t<NP, 128, 1, LEARNED>(p, sys, items, n_items, queue, shape.grid, smem, stream);
-    case 1282: return launch_batched_t<NP, 128, 2, LEARNED>(p, sys, items, n_items, queue, shape.grid, smem, stream);
-    case 2561: return launch_batched_t<NP, 256, 1, LEARNED>(p, sys, items, n_items, queue, shape.grid, smem, stream);
-    case 2562: return launch_batched_t<NP, 256, 2, LEARNED>(p, sys, items, n_items, queue, shape.grid, smem, stream);
+    case 641: return launch_batched_t<NP, 64, 1, LEARNED, KICK64>(p, sys, items, n_items, queue, g, smem, stream);
+    case 642: return launch_batched_t<NP, 64, 2, LEARNED, KICK64>(p, sys, items, n_items, queue, g, smem, stream);
+    case 1281: return launch_batched_t<NP, 128, 1, LEARNED, KICK64>(p, sys, items, n_items, queue, g, smem, stream);
+    case 1282: return launch_batched_t<NP, 128, 2, LEARNED, KICK64>(p, sys, items, n_items, queue, g, smem, stream);
+    case 2561: return launch_batched_t<NP, 256, 1, LEARNED, KICK64>(p, sys, items, n_items, queue, g, smem, stream);
+    case 2562: return launch_batched_t<NP, 256, 2, LEARNED, KICK64>(p, sys, items, n_items, queue, g, smem, stream);
     default: return cudaErrorInvalidValue;
     }
 }
 
+// One kernel variant: four planets besides the Sun specialised, other counts
+// on the generic planet loop.
+template <bool LEARNED, bool KICK64>
+cudaError_t launch_batched_variant(const Common& p, const BatchSystems& sys, const BatchItem* items,
+                                   const uint32_t* n_items, uint32_t* queue, uint32_t npl, const BatchShape& shape,
+                                   size_t smem, cudaStream_t stream)
+{
+    return npl == 5 ? launch_batched_np<4, LEARNED, KICK64>(p, sys, items, n_items, queue, shape, smem, stream)
+                    : launch_batched_np<0, LEARNED, KICK64>(p, sys, items, n_items, queue, shape, smem, stream);
+}
+
 }  // namespace
 
-// Learned-starter launch (batched_learned.cu).
-cudaError_t launch_batched_learned(const tile::Common& p, const BatchSystems& sys, const BatchItem* items,
-                                   const uint32_t* n_items, uint32_t* queue, uint32_t npl, const BatchShape& shape,
-                                   size_t smem, cudaStream_t stream);
+// Launches of the variants compiled in other translation units (one variant
+// per unit): plain starters with the FP64 kick (batched_kick64.cu), the
+// learned starter with the float-float kick (batched_learned.cu) and with the
+// FP64 kick (batched_learned_kick64.cu).
+#define GLISSER_BATCHED_VARIANT_LAUNCH(name)                                                                     \
+    cudaError_t name(const tile::Common& p, const BatchSystems& sys, const BatchItem* items,                     \
+                     const uint32_t* n_items, uint32_t* queue, uint32_t npl, const BatchShape& shape, size_t smem, \
+                     cudaStream_t stream)
+GLISSER_BATCHED_VARIANT_LAUNCH(launch_batched_kick64);
+GLISSER_BATCHED_VARIANT_LAUNCH(launch_batched_learned);
+GLISSER_BATCHED_VARIANT_LAUNCH(launch_batched_learned_kick64);
 
 }  // namespace glisser

@@ -246,6 +246,16 @@ int glisser_set_kepler_tolerance(glisser_t* h, double tol)
     });
 }
 
+int glisser_set_kick(glisser_t* h, int kick)
+{
+    if (kick != GLISSER_KICK_FLOAT_FLOAT && kick != GLISSER_KICK_FP64)
+        return fail(h, GLISSER_E_INVALID, "glisser_set_kick: GLISSER_KICK_FLOAT_FLOAT or GLISSER_KICK_FP64");
+    return guarded(h, [&] {
+        exec_of(h).set_kick(kick);
+        return GLISSER_OK;
+    });
+}
+
 int glisser_set_device_output(glisser_t* h, int on)
 {
     return guarded(h, [&] {
@@ -557,6 +567,20 @@ int glisser_stats(const glisser_t* h, unsigned long long* particle_steps, unsign
     return GLISSER_OK;
 }
 
+int glisser_borderline(const glisser_t* h, unsigned long long* tests)
+{
+    if (!h || !tests) return GLISSER_E_INVALID;
+    *tests = h->ex->borderline_tests();
+    return GLISSER_OK;
+}
+
+int glisser_learned_drifts(const glisser_t* h, unsigned long long* drifts)
+{
+    if (!h || !drifts) return GLISSER_E_INVALID;
+    *drifts = h->ex->learned_drifts();
+    return GLISSER_OK;
+}
+
 int glisser_launches(const glisser_t* h, unsigned long long* launches)
 {
     if (!h || !launches) return GLISSER_E_INVALID;
@@ -767,6 +791,71 @@ int glisser_ensemble_stats(const glisser_ensemble_t* e, unsigned long long* part
     return GLISSER_OK;
 }
 
+int glisser_ensemble_set_state(glisser_ensemble_t* e, size_t n, const double* r, const double* v)
+{
+    if (!e || (n && (!r || !v))) return fail(nullptr, GLISSER_E_INVALID, "glisser_ensemble_set_state: bad arguments");
+    return guarded_e([&] {
+        e->e->put_state(n, r, v);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_ensemble_get_state(glisser_ensemble_t* e, double* r, double* v, uint16_t* flags, size_t cap, size_t* n)
+{
+    if (!e) return GLISSER_E_INVALID;
+    return guarded_e([&] {
+        if (n) *n = e->e->particles_total();
+        if (r || v || flags) e->e->take_state(cap, r, v, flags);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_ensemble_stream(const glisser_ensemble_t* e, void** stream)
+{
+    if (!e || !stream) return GLISSER_E_INVALID;
+    *stream = e->e->stream();
+    return GLISSER_OK;
+}
+
+int glisser_ensemble_get_deaths(const glisser_ensemble_t* e, size_t s, double* deathtime, uint32_t* deathtime_index,
+                                size_t cap, size_t* n)
+{
+    if (!e) return GLISSER_E_INVALID;
+    return guarded_e([&] {
+        std::vector<double> dt;
+        std::vector<uint32_t> di;
+        e->e->deaths(s, dt, di);
+        if (n) *n = dt.size();
+        const size_t k = std::min(cap, dt.size());
+        if (deathtime) std::copy(dt.begin(), dt.begin() + k, deathtime);
+        if (deathtime_index) std::copy(di.begin(), di.begin() + k, deathtime_index);
+        return GLISSER_OK;
+    });
+}
+
+int glisser_ensemble_borderline(const glisser_ensemble_t* e, unsigned long long* tests)
+{
+    if (!e || !tests) return GLISSER_E_INVALID;
+    *tests = e->e->borderline_tests();
+    return GLISSER_OK;
+}
+
+int glisser_ensemble_learned_drifts(const glisser_ensemble_t* e, unsigned long long* drifts)
+{
+    if (!e || !drifts) return GLISSER_E_INVALID;
+    *drifts = e->e->learned_drifts();
+    return GLISSER_OK;
+}
+
+int glisser_ensemble_set_kick(glisser_ensemble_t* e, int kick)
+{
+    if (!e) return GLISSER_E_INVALID;
+    if (kick != GLISSER_KICK_FLOAT_FLOAT && kick != GLISSER_KICK_FP64)
+        return fail(nullptr, GLISSER_E_INVALID, "glisser_ensemble_set_kick: GLISSER_KICK_FLOAT_FLOAT or GLISSER_KICK_FP64");
+    e->e->set_kick(kick);
+    return GLISSER_OK;
+}
+
 int glisser_ensemble_time(const glisser_ensemble_t* e, double* t)
 {
     if (!e || !t) return GLISSER_E_INVALID;
@@ -832,6 +921,13 @@ int glisser_mlp_log_states(glisser_mlp_t* m, const glisser_particles* pa, size_t
         if (n_logged) *n_logged = k;
         return GLISSER_OK;
     });
+}
+
+int glisser_mlp_set_log_floor(glisser_mlp_t* m, double tau2_min)
+{
+    if (!m || !(tau2_min >= 0)) return fail(nullptr, GLISSER_E_INVALID, "glisser_mlp_set_log_floor: bad arguments");
+    m->t->set_log_floor(tau2_min);
+    return GLISSER_OK;
 }
 
 int glisser_mlp_add_samples(glisser_mlp_t* m, const float* feat, const float* target, size_t n)
@@ -951,6 +1047,13 @@ int glisser_mlp_save(const glisser_mlp_t* m, const char* path)
         if (!o) throw glisser::IoError(std::string("cannot write ") + path);
         return GLISSER_OK;
     });
+}
+
+int glisser_mlp_pack(const float* params, uint32_t* w1p, uint32_t* w2p)
+{
+    if (!params || !w1p || !w2p) return fail(nullptr, GLISSER_E_INVALID, "glisser_mlp_pack: bad arguments");
+    glisser::mlp_pack(params, w1p, w2p);
+    return GLISSER_OK;
 }
 
 int glisser_mlp_device_weights(glisser_mlp_t* m, const void** dev)

@@ -32,6 +32,7 @@
 
 #include "config.h"
 #include "ensemble.h"
+#include "parallel.h"
 #include "executor.h"
 #include "mlp_train.h"
 #include "planets_dev.h"
@@ -95,6 +96,7 @@ struct Ensemble::Dev {
     uint32_t graph_len[2] = {};
     int graph_starter[2] = { -1, -1 };
     double graph_tol[2] = { -1, -1 };
+    int graph_kick[2] = { -1, -1 };
     void* d_mlp = nullptr;            // learned-starter weights
     // device planet integrator state ([S][npl] arrays, one allocation)
     PlanetSysDev pl{};
@@ -104,9 +106,13 @@ struct Ensemble::Dev {
     cudaStream_t pstream = nullptr;
     cudaEvent_t planets_done = nullptr;
     int mlp_version = 0, graph_mlp[2] = { 0, 0 };
+    double* h_state = nullptr;        // pinned staging of whole-ensemble state transfers
+    uint16_t* h_state_flags = nullptr;
 
     ~Dev()
     {
+        cudaFreeHost(h_state);
+        cudaFreeHost(h_state_flags);
         mlp_free(d_mlp);
         cudaFree(pl_base);
         cudaFreeHost(h_status);
@@ -356,6 +362,8 @@ void Ensemble::init()
     n_ = total;
     std::vector<double> col(9 * std::max<size_t>(total, 1));
     flags_.assign(total, 0);
+    deathtime_.assign(total, 0.0);
+    dti_.assign(total, 0u);
     ids_.resize(total);
     for (size_t s = 0; s < sys_.size(); s++) {
         System& y = sys_[s];
@@ -386,9 +394,10 @@ void Ensemble::init()
             c[g] = r.x; c[total + g] = r.y; c[2 * total + g] = r.z;
             c[3 * total + g] = v.x; c[4 * total + g] = v.y; c[5 * total + g] = v.z;
             c[6 * total + g] = a.x; c[7 * total + g] = a.y; c[8 * total + g] = a.z;
-            // a particle inside an encounter radius at start is removed at the
-            // first block end, as the executor's KillEncounter does
-            flags_[g] = (fl & 0x01) ? (uint16_t)((fl & 0xFF00) | 0x80) : fl;
+            // flagged at start: out of the integration with deathtime 0, its
+            // flag kept as set here (as the executor and the reference's
+            // initial partition leave it, src/executor.cu:181-187)
+            flags_[g] = fl;
             ids_[g] = (uint32_t)k;
         }
         alive_.push_back(0);
@@ -440,9 +449,9 @@ void Ensemble::init()
         d.h_nitems[b] = hmalloc<uint32_t>(1, "pinned");
     }
     d.d_ctr = dmalloc<uint32_t>(8, "cudaMalloc counters");
-    d.d_evals = dmalloc<unsigned long long>(1, "cudaMalloc evals");
+    d.d_evals = dmalloc<unsigned long long>(3, "cudaMalloc evals");
     d.h_ctr = hmalloc<uint32_t>(8, "pinned");
-    d.h_evals = hmalloc<unsigned long long>(1, "pinned");
+    d.h_evals = hmalloc<unsigned long long>(3, "pinned");
     d.d_ho_index = dmalloc<uint32_t>(cap, "cudaMalloc hand-off");
     d.d_ho_id = dmalloc<uint32_t>(cap, "cudaMalloc hand-off");
     d.d_ho_dti = dmalloc<uint32_t>(cap, "cudaMalloc hand-off");
@@ -525,7 +534,7 @@ void Ensemble::enqueue(int par)
                        d.stream), "items");
     ck(cudaMemcpyAsync(d.d_nitems[par], d.h_nitems[par], sizeof(uint32_t), cudaMemcpyHostToDevice, d.stream), "n");
     ck(cudaMemsetAsync(d.d_ctr, 0, 8 * sizeof(uint32_t), d.stream), "memset");
-    ck(cudaMemsetAsync(d.d_evals, 0, sizeof(unsigned long long), d.stream), "memset");
+    ck(cudaMemsetAsync(d.d_evals, 0, 3 * sizeof(unsigned long long), d.stream), "memset");
     BatchSystems sy{ d.d_log[par], log_stride_, d.d_m[par], d.d_rh[par], d.d_id[par] };
     glisser_step_params sp{};
     sp.dt = cfg.dt;
@@ -534,6 +543,7 @@ void Ensemble::enqueue(int par)
     sp.kill_encounters = 1;
     sp.mlp = starter_ == GLISSER_STARTER_LEARNED ? d.d_mlp : nullptr;
     sp.kepler_tol = kepler_tol_;
+    sp.kick = kick_;
     glisser_handoff ho{};
     ho.count = d.d_ctr;
     ho.status = d.d_ctr + 1;
@@ -543,11 +553,14 @@ void Ensemble::enqueue(int par)
     ho.deathtime_index = d.d_ho_dti;
     ho.capacity = (uint32_t)std::max<size_t>(n_, 1);
     ho.evals = d.d_evals;
+    ho.borderline = d.d_evals + 1;
+    ho.learned = d.d_evals + 2;
     int rc = launch_batched(&d.pa, sy, d.d_items[par], d.d_nitems[par], d.d_ctr + 2, npl_, len_, &sp, &ho, shape_,
                             d.stream);
     if (rc != GLISSER_OK) throw CudaError(std::string("batched launch failed: ") + timeblock_error());
     ck(cudaMemcpyAsync(d.h_ctr, d.d_ctr, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, d.stream), "counters");
-    ck(cudaMemcpyAsync(d.h_evals, d.d_evals, sizeof(unsigned long long), cudaMemcpyDeviceToHost, d.stream), "evals");
+    ck(cudaMemcpyAsync(d.h_evals, d.d_evals, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, d.stream),
+       "evals");
 }
 
 double Ensemble::step(double* gpu_ms)
@@ -572,7 +585,8 @@ double Ensemble::step(double* gpu_ms)
             const BatchShape& gs = d.graph_shape[par];
             bool stale = !d.graph[par] || gs.cta != shape_.cta || gs.ppt != shape_.ppt || gs.grid != shape_.grid ||
                          d.graph_len[par] != len_ || d.graph_starter[par] != starter_ ||
-                         d.graph_mlp[par] != d.mlp_version || d.graph_tol[par] != kepler_tol_;
+                         d.graph_mlp[par] != d.mlp_version || d.graph_tol[par] != kepler_tol_ ||
+                         d.graph_kick[par] != kick_;
             if (stale) {
                 if (d.graph[par]) cudaGraphExecDestroy(d.graph[par]);
                 d.graph[par] = nullptr;
@@ -587,6 +601,7 @@ double Ensemble::step(double* gpu_ms)
                 d.graph_starter[par] = starter_;
                 d.graph_mlp[par] = d.mlp_version;
                 d.graph_tol[par] = kepler_tol_;
+                d.graph_kick[par] = kick_;
             }
             ck(cudaGraphLaunch(d.graph[par], d.stream), "graph launch");
             launches_ += 1;
@@ -607,17 +622,22 @@ double Ensemble::step(double* gpu_ms)
         ck(cudaEventElapsedTime(&ms, d.k0, d.k1), "elapsed");
         if (d.h_ctr[1]) throw CudaError("batched kernel reported a planet-log staging timeout");
         uint32_t k = std::min<uint32_t>(d.h_ctr[0], (uint32_t)std::max<size_t>(n_, 1));
-        evals_ += *d.h_evals;
+        evals_ += d.h_evals[0];
+        borderline_ += d.h_evals[1];
+        learned_ += d.h_evals[2];
         uint64_t dti_sum = 0;
         if (k) {
             ck(cudaMemcpy(d.h_ho_index, d.d_ho_index, k * sizeof(uint32_t), cudaMemcpyDeviceToHost), "hand-off");
             ck(cudaMemcpy(d.h_ho_dti, d.d_ho_dti, k * sizeof(uint32_t), cudaMemcpyDeviceToHost), "hand-off");
             ck(cudaMemcpy(d.h_ho_flags, d.d_ho_flags, k * sizeof(uint16_t), cudaMemcpyDeviceToHost), "hand-off");
+            const float tf = (float)t;     // block end, stamped as the executor does
             for (uint32_t q = 0; q < k; q++) {
                 uint32_t g = d.h_ho_index[q];
                 bool was_alive = flags_[g] == 0;
                 flags_[g] = d.h_ho_flags[q];
                 dti_sum += d.h_ho_dti[q];
+                deathtime_[g] = tf;
+                dti_[g] = d.h_ho_dti[q];
                 if (was_alive && flags_[g] != 0) {
                     // locate the tile and the system of particle g
                     size_t t = std::upper_bound(tile_first_.begin(), tile_first_.end(), g) - tile_first_.begin() - 1;
@@ -658,6 +678,68 @@ void Ensemble::particles(size_t s, std::vector<Vec3>& r, std::vector<Vec3>& v, s
         r[k] = Vec3{ c[k], c[y.n + k], c[2 * y.n + k] };
         v[k] = Vec3{ c[3 * y.n + k], c[4 * y.n + k], c[5 * y.n + k] };
     }
+}
+
+void* Ensemble::stream() const { return dev_ ? (void*)dev_->stream : nullptr; }
+
+void Ensemble::ensure_state_staging()
+{
+    Dev& d = *dev_;
+    if (d.h_state) return;
+    d.h_state = hmalloc<double>(6 * std::max<size_t>(n_, 1), "pinned state");
+    d.h_state_flags = hmalloc<uint16_t>(std::max<size_t>(n_, 1), "pinned state");
+}
+
+void Ensemble::put_state(size_t n, const double* r, const double* v)
+{
+    if (!initialized_) throw std::runtime_error("put_state before init");
+    if (n != n_) throw std::invalid_argument("put_state: particle count differs from the ensemble's");
+    ensure_state_staging();
+    Dev& d = *dev_;
+    double* st = d.h_state;
+    parallel_for(n, [&](size_t b, size_t e) {
+        for (size_t k = b; k < e; k++) {
+            st[k] = r[3 * k]; st[n + k] = r[3 * k + 1]; st[2 * n + k] = r[3 * k + 2];
+            st[3 * n + k] = v[3 * k]; st[4 * n + k] = v[3 * k + 1]; st[5 * n + k] = v[3 * k + 2];
+        }
+    });
+    double* dst[6] = { d.pa.rx, d.pa.ry, d.pa.rz, d.pa.vx, d.pa.vy, d.pa.vz };
+    for (int k = 0; k < 6; k++)
+        ck(cudaMemcpyAsync(dst[k], st + k * n, n * sizeof(double), cudaMemcpyHostToDevice, d.stream), "upload state");
+    // the next block's kernel runs on the same stream, after the copies
+}
+
+void Ensemble::take_state(size_t cap, double* r, double* v, uint16_t* flags)
+{
+    if (!initialized_) throw std::runtime_error("take_state before init");
+    if (cap < n_) throw std::invalid_argument("take_state: room for fewer particles than the ensemble holds");
+    ensure_state_staging();
+    Dev& d = *dev_;
+    const size_t n = n_;
+    double* st = d.h_state;
+    const double* src[6] = { d.pa.rx, d.pa.ry, d.pa.rz, d.pa.vx, d.pa.vy, d.pa.vz };
+    for (int k = 0; k < 6; k++)
+        ck(cudaMemcpyAsync(st + k * n, src[k], n * sizeof(double), cudaMemcpyDeviceToHost, d.stream), "download state");
+    if (flags)
+        ck(cudaMemcpyAsync(d.h_state_flags, d.pa.flags, n * sizeof(uint16_t), cudaMemcpyDeviceToHost, d.stream),
+           "download flags");
+    ck(cudaStreamSynchronize(d.stream), "download sync");
+    parallel_for(n, [&](size_t b, size_t e) {
+        for (size_t k = b; k < e; k++) {
+            if (r) { r[3 * k] = st[k]; r[3 * k + 1] = st[n + k]; r[3 * k + 2] = st[2 * n + k]; }
+            if (v) { v[3 * k] = st[3 * n + k]; v[3 * k + 1] = st[4 * n + k]; v[3 * k + 2] = st[5 * n + k]; }
+            if (flags) flags[k] = d.h_state_flags[k];
+        }
+    });
+}
+
+void Ensemble::deaths(size_t s, std::vector<double>& deathtime, std::vector<uint32_t>& dti) const
+{
+    if (s >= sys_.size()) throw std::invalid_argument("system index out of range");
+    if (!initialized_) throw std::runtime_error("deaths before init");
+    const System& y = sys_[s];
+    deathtime.assign(deathtime_.begin() + y.start, deathtime_.begin() + y.start + y.n);
+    dti.assign(dti_.begin() + y.start, dti_.begin() + y.start + y.n);
 }
 
 // One wave of persistent CTAs at the occupancy the kernel reaches.

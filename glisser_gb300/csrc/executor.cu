@@ -664,9 +664,9 @@ void Executor::init()
     }
     size_t cap = std::max<size_t>(n, 1);
     ck(cudaMalloc(&d.d_ctr, 16 * sizeof(uint32_t)), "cudaMalloc counters");
-    ck(cudaMalloc(&d.d_evals, sizeof(unsigned long long)), "cudaMalloc evals");
+    ck(cudaMalloc(&d.d_evals, 3 * sizeof(unsigned long long)), "cudaMalloc evals");
     ck(cudaMallocHost(&d.h_ctr, 16 * sizeof(uint32_t)), "pinned");
-    ck(cudaMallocHost(&d.h_evals, sizeof(unsigned long long)), "pinned");
+    ck(cudaMallocHost(&d.h_evals, 3 * sizeof(unsigned long long)), "pinned");
     ck(cudaMalloc(&d.d_ho_index, cap * sizeof(uint32_t)), "cudaMalloc hand-off");
     ck(cudaMalloc(&d.d_ho_id, cap * sizeof(uint32_t)), "cudaMalloc hand-off");
     ck(cudaMalloc(&d.d_ho_dti, cap * sizeof(uint32_t)), "cudaMalloc hand-off");
@@ -720,7 +720,8 @@ bool Executor::step_block(double* cpu_ms, double* gpu_ms)
         launches_total_ += 3;   // count, scan, scatter
         if (rc != GLISSER_OK) throw CudaError("partition launch failed");
         ck(cudaMemcpyAsync(d.h_ctr, d.d_ctr, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, d.main), "counters");
-        ck(cudaMemcpyAsync(d.h_evals, d.d_evals, sizeof(unsigned long long), cudaMemcpyDeviceToHost, d.main), "evals");
+        ck(cudaMemcpyAsync(d.h_evals, d.d_evals, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, d.main),
+           "evals");
         ck(cudaEventRecord(d.done, d.main), "event");
         d.cur = nxt;
         host_dirty_ = true;
@@ -728,7 +729,7 @@ bool Executor::step_block(double* cpu_ms, double* gpu_ms)
     };
     if (n_range > 0) {
         ck(cudaMemsetAsync(d.d_ctr, 0, 16 * sizeof(uint32_t), d.main), "memset counters");
-        ck(cudaMemsetAsync(d.d_evals, 0, sizeof(unsigned long long), d.main), "memset evals");
+        ck(cudaMemsetAsync(d.d_evals, 0, 3 * sizeof(unsigned long long), d.main), "memset evals");
     }
     if (n_kernel > 0) {
         ck(cudaStreamWaitEvent(d.main, d.uploaded[used], 0), "wait upload");
@@ -747,6 +748,7 @@ bool Executor::step_block(double* cpu_ms, double* gpu_ms)
         sp.kill_encounters = cfg.resolve_encounters ? GLISSER_ENCOUNTERS_ROLLBACK : GLISSER_ENCOUNTERS_KILL;
         sp.mlp = starter_ == GLISSER_STARTER_LEARNED ? d.d_mlp : nullptr;
         sp.kepler_tol = kepler_tol_;
+        sp.kick = kick_;
         glisser_handoff ho{};
         ho.count = d.d_ctr;
         ho.status = d.d_ctr + 1;
@@ -756,6 +758,8 @@ bool Executor::step_block(double* cpu_ms, double* gpu_ms)
         ho.deathtime_index = d.d_ho_dti;
         ho.capacity = (uint32_t)std::max<size_t>(pa_.n, 1);
         ho.evals = d.d_evals;
+        ho.borderline = d.d_evals + 1;
+        ho.learned = d.d_evals + 2;
         ck(cudaEventRecord(d.start, d.main), "event");
         int rc = launch_timeblock(&d.buf[d.cur].p, n_kernel, &pb, &sp, &ho, d.main);
         if (rc != GLISSER_OK) throw CudaError(std::string("time-block launch failed: ") + timeblock_error());
@@ -788,7 +792,9 @@ bool Executor::step_block(double* cpu_ms, double* gpu_ms)
         if (status) throw CudaError("time-block kernel reported a planet-log staging timeout");
         uint32_t n0 = d.h_ctr[2], n1 = d.h_ctr[3];
         uint32_t k = std::min<uint32_t>(d.h_ctr[0], (uint32_t)std::max<size_t>(pa_.n, 1));
-        evals_total_ += *d.h_evals;
+        evals_total_ += d.h_evals[0];
+        borderline_total_ += d.h_evals[1];
+        learned_total_ += d.h_evals[2];
         // both particle buffers must agree on the particles that left the
         // partitioned range this block (the next partition reads only one)
         if (n0 + n1 < n_range) {

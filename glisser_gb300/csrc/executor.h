@@ -73,6 +73,9 @@ public:
     void set_device_interp(bool on) { device_interp_ = on; }
     // Kepler residual tolerance |f| < tol * dt of the drift (0: 1e-13).
     void set_kepler_tolerance(double tol) { kepler_tol_ = tol; }
+    // Arithmetic of the planet kick and its radius tests (GLISSER_KICK_*).
+    void set_kick(int kick) { kick_ = kick; }
+    int kick() const { return kick_; }
     // Track snapshots built on the device (default) or by the host writer.
     void set_device_output(bool on) { device_output_ = on; }
     // Writes a track snapshot with the particle records built on the device
@@ -80,6 +83,10 @@ public:
     // initialised, no device particles, sparse ids, or switched off).
     bool write_track_device(std::ostream& out, double* ms = nullptr);
     unsigned long long kepler_evals() const { return evals_total_; }
+    // threshold-borderline radius tests (glisser_handoff.borderline) since init
+    unsigned long long borderline_tests() const { return borderline_total_; }
+    // drifts started from the learned starter's network guess since init
+    unsigned long long learned_drifts() const { return learned_total_; }
     unsigned long long particle_steps() const { return psteps_total_; }
     unsigned long long launches() const { return launches_total_; }
     void* stream() const;
@@ -114,9 +121,10 @@ private:
     int starter_ = GLISSER_STARTER_SERIES;
     bool device_interp_ = true;
     double kepler_tol_ = 0;
+    int kick_ = GLISSER_KICK_FLOAT_FLOAT;
     bool device_output_ = true;
     uint32_t max_id_ = 0;
-    unsigned long long evals_total_ = 0;
+    unsigned long long evals_total_ = 0, borderline_total_ = 0, learned_total_ = 0;
     unsigned long long psteps_total_ = 0;
     unsigned long long launches_total_ = 0;
 

@@ -25,16 +25,17 @@
 //    the reverted correction through fifth order provably lands within it
 //    (bounds on the dropped terms and on the FP32 rounding): the
 //    correction is then folded to third order.  A starter within ~1e-4 of
-//    the root (the learned one) so needs one Stumpff evaluation, not two;
+//    the root (the learned one, the FP32 pre-solve) so needs one Stumpff
+//    evaluation, not two;
 //  * the default starter is a tenth-order reversion of the time series of
 //    Kepler's equation, accurate to ~1e-16 for steps well inside an orbit,
 //    so the residual test normally accepts it on the first evaluation: one
 //    Stumpff evaluation per drift;
 //  * threshold tests on non-negative values compare the IEEE bit patterns as
 //    integers (same answer, including NaN, but on the integer pipe);
-//  * in the FP64-bound kernels the accepted correction's fold and the
-//    float-float sums return to FP64 by integer additions to the bit
-//    patterns (f64_add_tiny, ff_to_f64 in fastmath.cuh);
+//  * the accepted correction's fold and the float-float sums return to FP64
+//    by integer additions to the bit patterns (f64_add_tiny, ff_to_f64 in
+//    fastmath.cuh);
 //  * the Stumpff series is evaluated by Horner in x = alpha s^2; arguments
 //    with |x| >= 0.1 are quartered and rebuilt with the double-angle
 //    identities (c0,c1,c2,c3 as in Danby eq. 6.9.15).
@@ -54,7 +55,7 @@ constexpr int KEP_LAGUERRE_MAX = 200;   // bounded fallback passes
 enum Starter : int {
     STARTER_CLASSIC = 0,   // the reference's kepu_guess (src/wh.cpp:188-220)
     STARTER_SERIES = 1,    // tenth-order time-series reversion, else FP32 Kepler pre-solve
-    STARTER_LEARNED = 2,   // MLP over drift invariants, classic fallback
+    STARTER_LEARNED = 2,   // series where it applies, else the MLP over drift invariants; classic restart
 };
 
 // G1, G2, G3 of one Stumpff evaluation; G0 = 1 - alpha G2 is formed where a
@@ -90,12 +91,9 @@ __device__ __forceinline__ void stumpff_short(double x, double& c2, double& c3)
     c3 = fma(x, fma(x, fma(x, -1.0 / 362880.0, 1.0 / 5040.0), -1.0 / 120.0), 1.0 / 6.0);
 }
 
-// FP64_BOUND (here and in the solver below): the kernel is bound by the
-// FP64 pipe, so float-to-double sums and the residual-accepted fold go
-// through the integer pipe (ff_to_f64, f64_add_tiny); otherwise (the learned
-// kernels, bound by the network's FP32 work and issue, with no registers to
-// spare) they stay FP64 additions, which measured faster there.
-template <bool FP64_BOUND>
+// The time-block kernels are bound by the FP64 pipe, so here and in the
+// solver below float-to-double sums and the residual-accepted fold go through
+// the integer pipe (ff_to_f64, f64_add_tiny).
 __device__ __forceinline__ GFun gfuns(double s, double alpha)
 {
     double s2 = s * s;
@@ -116,7 +114,7 @@ __device__ __forceinline__ GFun gfuns(double s, double alpha)
         const ff c3f = ff_add_f(ff_sixth(), xf * fmaf(xf, 1.0f / 5040.0f, -1.0f / 120.0f));
         const ff g3f = ff_mul(ff_mul(sf, ff_sqr(sf)), c3f);
         g.g2 = s2 * c2;
-        g.g3 = FP64_BOUND ? ff_to_f64(g3f) : f64_of_f32(g3f.hi) + f64_of_f32(g3f.lo);
+        g.g3 = ff_to_f64(g3f);
         g.g1 = fma(-alpha, g.g3, s);
         return g;
     } else if (__all_sync(lanes, lt_nonneg(ax, 2e-3))) {
@@ -386,7 +384,6 @@ __device__ __forceinline__ int newton_terms(double f, double fp, double h, doubl
 // below ~3 tol of the G-function it corrects and needs only a float's
 // precision -- the products are FP32 and enter through f64_add_tiny (the
 // FP64 fold when ds or a product is outside the float range).
-template <bool FP64_BOUND>
 __device__ __forceinline__ void fold_small(GFun& g, double& ds, double f, double r0, double u, double mu,
                                            double alpha)
 {
@@ -397,15 +394,9 @@ __device__ __forceinline__ void fold_small(GFun& g, double& ds, double f, double
     const float c3 = dsf * g2f, c2 = dsf * g1f, c1 = dsf * g0f;
     if (f32_mid_range(fpf) && f32_mid_range(c3) && f32_mid_range(c2) && f32_mid_range(c1)) {
         ds = f64_of_f32(dsf);
-        if constexpr (FP64_BOUND) {
-            g.g3 = f64_add_tiny(g.g3, c3);
-            g.g2 = f64_add_tiny(g.g2, c2);
-            g.g1 = f64_add_tiny(g.g1, c1);
-        } else {
-            g.g3 += f64_of_f32(c3);
-            g.g2 += f64_of_f32(c2);
-            g.g1 += f64_of_f32(c1);
-        }
+        g.g3 = f64_add_tiny(g.g3, c3);
+        g.g2 = f64_add_tiny(g.g2, c2);
+        g.g1 = f64_add_tiny(g.g1, c1);
     } else {
         const double g0 = gfun_g0(g, alpha);
         ds = -f / fma(r0, g0, fma(u, g.g1, mu * g.g2));
@@ -429,16 +420,15 @@ __device__ __forceinline__ void fold_small(GFun& g, double& ds, double f, double
 //       G2 + ds (G1 + ds/2 (G0 - alpha ds/3 G1)),
 //       G1 + ds (G0 - alpha ds/2 (G1 + ds/3 G0));
 //     the dropped terms are below ~(ds/s)^4 ~ 1e-16 of G.
-template <bool FP64_BOUND>
 __device__ __forceinline__ bool kepler_newton(double& s, double dt, double r0, double u, double mu, double alpha,
                                               double tol, GFun& g, double& ds, uint16_t& evals)
 {
     for (int it = 0; it < KEP_NEWTON_MAX; it++) {
-        g = gfuns<FP64_BOUND>(s, alpha);
+        g = gfuns(s, alpha);
         evals++;
         double f = fma(r0, g.g1, fma(u, g.g2, fma(mu, g.g3, -dt)));
         if (lt_nonneg(fabs(f), tol)) {
-            fold_small<FP64_BOUND>(g, ds, f, r0, u, mu, alpha);
+            fold_small(g, ds, f, r0, u, mu, alpha);
             return true;
         }
         const double g0 = gfun_g0(g, alpha);
@@ -468,14 +458,13 @@ __device__ __forceinline__ bool kepler_newton(double& s, double dt, double r0, d
 // f'' = (mu - alpha r0) G1 + u G0), at most KEP_LAGUERRE_MAX passes; same
 // outputs as kepler_newton (the accepted correction folded to first order in
 // FP64).
-template <bool FP64_BOUND>
 __device__ __forceinline__ bool kepler_laguerre(double& s, double dt, double r0, double u, double mu, double alpha,
                                              double tol, GFun& g, double& ds, uint16_t& evals)
 {
     const double ln = 5.0;
     const double k = fma(-alpha, r0, mu);
     for (int it = 0; it < KEP_LAGUERRE_MAX; it++) {
-        g = gfuns<FP64_BOUND>(s, alpha);
+        g = gfuns(s, alpha);
         evals++;
         const double g0 = gfun_g0(g, alpha);
         double f = fma(r0, g.g1, fma(u, g.g2, fma(mu, g.g3, -dt)));
@@ -520,11 +509,13 @@ __device__ __forceinline__ DriftInvariants drift_invariants(double rx, double ry
 // enters the energy alpha = 2 mu / r0 - v^2 of the next drift, where near
 // pericentre of an eccentric orbit any inconsistency with the vector is
 // magnified).  tol_dt = the residual tolerance times dt (KEP_TOL * dt by
-// default).  LEARNED: `guess` is the network's starting s (non-positive
-// outside its training box, where the classic starter runs; the classic
-// starter is also the restart when the Newton passes from the network's
-// guess do not converge); otherwise `starter` picks the classic or the
-// series starter.
+// default).  LEARNED: `guess` is the network's starting s where the kernel
+// ran the network (drifts with tau^2 >= SERIES_TAU2_MAX inside its training
+// box); a non-positive guess takes the series rule below, and the classic
+// starter is the restart when the Newton passes from the network's guess do
+// not converge.  Otherwise `starter` picks the classic or the series rule
+// (the tenth-order series while tau^2 < SERIES_TAU2_MAX, else the FP32
+// Kepler pre-solve for bound orbits and the classic starter for unbound ones).
 template <bool LEARNED>
 __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, double& rz, double& vx, double& vy, double& vz,
                                                    double& r2_io, double& rinv_io, const DriftInvariants& q, double dt,
@@ -538,9 +529,9 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
 
     double s;
     [[maybe_unused]] bool from_mlp = false;
-    if constexpr (LEARNED) {
-        from_mlp = guess > 0;
-        s = from_mlp ? guess : starter_classic(dt, r0, rinv, mu, alpha, u);
+    if constexpr (LEARNED) from_mlp = guess > 0;
+    if (from_mlp) {
+        s = guess;
     } else if (starter == STARTER_CLASSIC) {
         s = starter_classic(dt, r0, rinv, mu, alpha, u);
     } else {
@@ -552,14 +543,14 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
     const double tol = tol_dt;
     GFun g;
     double ds = 0;
-    bool ok = kepler_newton<!LEARNED>(s, dt, r0, u, mu, alpha, tol, g, ds, res.evals);
+    bool ok = kepler_newton(s, dt, r0, u, mu, alpha, tol, g, ds, res.evals);
     if constexpr (LEARNED) {
         if (!ok && from_mlp) {
             s = starter_classic(dt, r0, rinv, mu, alpha, u);
-            ok = kepler_newton<!LEARNED>(s, dt, r0, u, mu, alpha, tol, g, ds, res.evals);
+            ok = kepler_newton(s, dt, r0, u, mu, alpha, tol, g, ds, res.evals);
         }
     }
-    if (!ok) ok = kepler_laguerre<!LEARNED>(s, dt, r0, u, mu, alpha, tol, g, ds, res.evals);
+    if (!ok) ok = kepler_laguerre(s, dt, r0, u, mu, alpha, tol, g, ds, res.evals);
     if (!ok) res.flags |= 0x04;
     // g: the G-functions at the root (the last evaluation's when not converged)
     const double g3 = g.g3, g2 = g.g2, g1 = g.g1;
@@ -580,7 +571,8 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
 }
 
 // The same drift for a single particle: invariants and, LEARNED, the scalar
-// network (weights `mlp`) evaluated here.
+// network (weights `mlp`) evaluated here where the kernels run it (tau^2 at
+// or above SERIES_TAU2_MAX).
 template <bool LEARNED>
 __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, double& rz, double& vx, double& vy, double& vz,
                                                    double& r2_io, double& rinv_io, double dt, double mu, int starter,
@@ -588,7 +580,9 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
 {
     const DriftInvariants q = drift_invariants(rx, ry, rz, vx, vy, vz, r2_io, rinv_io, dt, mu);
     double guess = -1.0;
-    if constexpr (LEARNED) guess = starter_learned(mlp, q.T, rinv_io, q.tau2, q.u, q.mu_r, q.alpha);
+    if constexpr (LEARNED) {
+        if (!(q.tau2 < SERIES_TAU2_MAX)) guess = starter_learned(mlp, q.T, rinv_io, q.tau2, q.u, q.mu_r, q.alpha);
+    }
     return kepler_drift<LEARNED>(rx, ry, rz, vx, vy, vz, r2_io, rinv_io, q, dt, mu, starter, guess, tol_dt);
 }
 

@@ -302,4 +302,13 @@ __device__ __forceinline__ float mlp_forward_warp(const MlpDev* __restrict__ w, 
     return __ldg(&w->b3) + v;
 }
 
+// mlp_forward_warp as an out-of-line call, for kernels that run the network
+// only in a rarely taken branch: the call boundary keeps the network's
+// registers out of the allocation of the kernel's main path (what the call
+// needs is saved and restored around it, only when it is taken).
+static __device__ __noinline__ float mlp_forward_warp_call(const MlpDev* __restrict__ w, float x0, float x1, float x2)
+{
+    return mlp_forward_warp(w, x0, x1, x2);
+}
+
 }  // namespace glisser

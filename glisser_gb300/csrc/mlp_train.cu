@@ -54,9 +54,10 @@ __device__ __forceinline__ uint32_t mix32(uint64_t x)
 // One plain-method solve per state (classic starter, quartic Newton, Laguerre
 // fallback: the drift's own solver) with the invariants computed exactly as
 // the drift computes them.  Non-converged solves get a NaN target, which the
-// training kernel skips.
+// training kernel skips.  Only solves with f0 >= f0_min count towards
+// evals_sum (the ones the host keeps).
 __global__ void log_solves_kernel(glisser_particles pa, uint32_t n, double dt, double mu, float* feat, float* target,
-                                  unsigned long long* evals_sum)
+                                  unsigned long long* evals_sum, float f0_min)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t evals = 0;
@@ -77,11 +78,11 @@ __global__ void log_solves_kernel(glisser_particles pa, uint32_t n, double dt, d
         GFun g;
         double ds = 0;
         uint16_t ev = 0;
-        bool ok = kepler_newton<true>(s, dt, r0, u, mu, alpha, tol, g, ds, ev);
-        if (!ok) ok = kepler_laguerre<true>(s, dt, r0, u, mu, alpha, tol, g, ds, ev);
-        evals = ev;
+        bool ok = kepler_newton(s, dt, r0, u, mu, alpha, tol, g, ds, ev);
+        if (!ok) ok = kepler_laguerre(s, dt, r0, u, mu, alpha, tol, g, ds, ev);
         float f0, f1, f2;
         mlp_features(tau2_f32(dt * rinv, mu_r), u, rinv, mu_r, alpha, f0, f1, f2);
+        evals = f0 >= f0_min ? ev : 0u;
         const double sf = s + ds;
         feat[3 * (size_t)i] = f0;
         feat[3 * (size_t)i + 1] = f1;
@@ -383,6 +384,15 @@ MlpDev make_dev(const float* params, const MlpNorm& norm)
 
 }  // namespace
 
+void mlp_pack(const float* params, uint32_t* w1p, uint32_t* w2p)
+{
+    MlpNorm norm;
+    std::memset(&norm, 0, sizeof norm);
+    const MlpDev d = make_dev(params, norm);
+    std::memcpy(w1p, d.w1p, sizeof d.w1p);
+    std::memcpy(w2p, d.w2p, sizeof d.w2p);
+}
+
 void* mlp_upload(const std::vector<uint8_t>& file)
 {
     if (file.size() != sizeof(MlpFileHeader) + MLP_NPARAM * sizeof(float))
@@ -457,10 +467,32 @@ size_t MlpTrainer::log_states(const glisser_particles& pa, size_t n, double dt, 
     size_t m = std::min(n, cap_ - n_);
     if (m == 0) return 0;
     glisser_particles p = pa;
+    // f0 = log(tau) >= log(tau2_min) / 2
+    const float f0_min = log_tau2_min_ > 0 ? (float)(0.5 * std::log(log_tau2_min_)) : -INFINITY;
     log_solves_kernel<<<(unsigned)((m + 255) / 256), 256, 0, stream>>>(p, (uint32_t)m, dt, mu, d_feat_ + 3 * n_,
-                                                                        d_target_ + n_, d_evals_);
+                                                                        d_target_ + n_, d_evals_, f0_min);
     check(cudaGetLastError(), "log_solves_kernel");
     check(cudaStreamSynchronize(stream), "log_solves_kernel");
+    if (log_tau2_min_ > 0) {
+        // keep the solves at or above the floor, in their order
+        std::vector<float> f(3 * m), y(m);
+        check(cudaMemcpy(f.data(), d_feat_ + 3 * n_, f.size() * sizeof(float), cudaMemcpyDeviceToHost), "samples");
+        check(cudaMemcpy(y.data(), d_target_ + n_, y.size() * sizeof(float), cudaMemcpyDeviceToHost), "samples");
+        size_t k = 0;
+        for (size_t i = 0; i < m; i++) {
+            if (!(f[3 * i] >= f0_min)) continue;
+            f[3 * k] = f[3 * i];
+            f[3 * k + 1] = f[3 * i + 1];
+            f[3 * k + 2] = f[3 * i + 2];
+            y[k] = y[i];
+            k++;
+        }
+        if (k > 0) {
+            check(cudaMemcpy(d_feat_ + 3 * n_, f.data(), 3 * k * sizeof(float), cudaMemcpyHostToDevice), "samples");
+            check(cudaMemcpy(d_target_ + n_, y.data(), k * sizeof(float), cudaMemcpyHostToDevice), "samples");
+        }
+        m = k;
+    }
     n_ += m;
     return m;
 }

@@ -29,6 +29,11 @@ struct MlpFileHeader {
 int drift_states(const glisser_particles* pa, size_t n, double dt, double mu, int starter, const void* mlp,
                  uint32_t* evals, uint16_t* flags, cudaStream_t stream);
 
+// The tensor-core operands the inference routine reads, as the device copy
+// holds them: W1 as the layer-1 MMA's B pairs [32][4] and W2 as the hidden
+// layer's B pairs [32][16] (BF16 pairs, low half first).
+void mlp_pack(const float* params, uint32_t* w1p, uint32_t* w2p);
+
 // Device copy of a weights file (validated), and its release.
 void* mlp_upload(const std::vector<uint8_t>& file);
 void mlp_free(void* dev);
@@ -43,8 +48,12 @@ public:
     // Appends one sample per state: the features of the drift by dt from
     // (r, v) and the universal anomaly the plain method (classic starter,
     // FP64 Newton to the drift tolerance) converges to.  Returns the number
-    // appended (limited by the remaining capacity).
+    // appended (limited by the remaining capacity; with a floor set, only the
+    // drifts with tau^2 >= the floor are kept).
     size_t log_states(const glisser_particles& pa, size_t n, double dt, double mu, cudaStream_t stream);
+    // Logs only drifts with tau^2 = dt^2 mu / r0^3 >= tau2_min (0: all): the
+    // drifts where the kernels run the network.
+    void set_log_floor(double tau2_min) { log_tau2_min_ = tau2_min; }
     void add_samples(const float* feat, const float* target, size_t n);
     void get_samples(float* feat, float* target, size_t first, size_t n) const;
     size_t samples() const { return n_; }
@@ -83,6 +92,7 @@ private:
     std::vector<float> params_;
     bool dev_stale_ = true;
     int adam_t_ = 0;
+    double log_tau2_min_ = 0;
     cudaStream_t stream_ = nullptr;
 
     void ensure_partials(size_t blocks);

@@ -9,6 +9,8 @@
 // each tile recomputes its ranks and writes the 12 particle arrays to the
 // output buffer.  HBM traffic is one read of the flags plus one read and one
 // write of the 96-byte particle record.
+#include <cuda.h>
+
 #include <cstdio>
 #include <mutex>
 
@@ -199,20 +201,52 @@ namespace {
 
 // Device address of g_noalloc_counts per device.  In host code the array's
 // name is only a host-side stand-in; the address kernels need comes from
-// cudaGetSymbolAddress, resolved once per device with that device current.
+// cudaGetSymbolAddress, resolved with that device current.  The address
+// belongs to the context the library's module was loaded into, so it is
+// cached together with that context (the driver's cuCtxGetCurrent, reached
+// through the runtime's entry-point query so that the library needs no link
+// to the driver library) and looked up again when the current context
+// differs: after a cudaDeviceReset, or under another context of the same
+// device, a call resolves the array afresh instead of using a stale address.
 constexpr int NOALLOC_MAX_DEVICES = 64;
 std::mutex g_noalloc_mutex;
 uint32_t* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+CUcontext g_noalloc_ctx[NOALLOC_MAX_DEVICES] = {};
+
+using CtxGetCurrent = CUresult (*)(CUcontext*);
+
+CtxGetCurrent ctx_get_current()
+{
+    static CtxGetCurrent fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        return reinterpret_cast<CtxGetCurrent>(f);
+    }();
+    return fn;
+}
+
+CUcontext current_context()
+{
+    CUcontext c = nullptr;
+    CtxGetCurrent fn = ctx_get_current();
+    if (!fn || fn(&c) != CUDA_SUCCESS) return nullptr;
+    return c;
+}
 
 int noalloc_scratch(uint32_t** out)
 {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES) return GLISSER_E_CUDA;
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_ptr[dev]) {
+    const CUcontext ctx = current_context();
+    if (!g_noalloc_ptr[dev] || !ctx || ctx != g_noalloc_ctx[dev]) {
         void* ptr = nullptr;
         if (cudaGetSymbolAddress(&ptr, g_noalloc_counts) != cudaSuccess || !ptr) return GLISSER_E_CUDA;
         g_noalloc_ptr[dev] = static_cast<uint32_t*>(ptr);
+        g_noalloc_ctx[dev] = current_context();   // the context the lookup ran in
     }
     *out = g_noalloc_ptr[dev];
     return GLISSER_OK;

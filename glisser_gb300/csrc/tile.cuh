@@ -18,6 +18,7 @@ struct Common {
     double tol_dt;          // Kepler residual tolerance x dt
     int starter;
     int kill;
+    bool kick64;            // GLISSER_KICK_FP64: the FP64-kick kernels
     const MlpDev* mlp;
     glisser_handoff ho;
 };
@@ -104,11 +105,27 @@ struct CtaShared {
     double rh2[MAX_PLANETS];
     ff mff[MAX_PLANETS];        // m and rh^2 as float-floats for the kick
     ff rh2ff[MAX_PLANETS];
+    float rh2win[MAX_PLANETS];  // 2^-40 rh^2: the borderline window of the float-float radius test
     uint32_t id[MAX_PLANETS];
     uint64_t bar[2];
     int abort;
     uint32_t item;
 };
+
+// Threshold-borderline radius tests.  A flag is a discrete test of a squared
+// distance against a squared radius (src/wh.cu:151, 163-169), so two correct
+// evaluations that round differently can disagree for a particle sitting on
+// the threshold.  Every test whose outcome counts is checked for a compared
+// value within about 2^-40 (9e-13) of its threshold and counted: a zero count
+// over a run shows that no flag of that run could depend on the rounding (the
+// float-float kick's ~2^-48, or the last bits of an FP64 evaluation).
+// near_nonneg: x within 2^13 units in the last place of t (x, t >= 0), on the
+// integer pipe.
+__device__ __forceinline__ uint32_t near_nonneg(double x, double t)
+{
+    const long long d = __double_as_longlong(x) - __double_as_longlong(t);
+    return (unsigned long long)(d + 8192) <= 16384ull ? 1u : 0u;
+}
 
 // Pull of planet j, m dr / |dr|^3 with dr = r - r_j, added to the sum s,
 // and its encounter test (src/wh.cu:145-160): the first planet inside its
@@ -117,25 +134,54 @@ struct CtaShared {
 // are perturbations next to the Sun's pull, which the drift integrates in
 // FP64, and carry ~1e-13 of their own size.
 __device__ __forceinline__ void planet_kick(const ff* L, int j, ff rx, ff ry, ff rz, ff& sx, ff& sy, ff& sz,
-                                            uint16_t& flags, const CtaShared& sh)
+                                            uint16_t& flags, uint32_t& border, const CtaShared& sh)
 {
     const ff dx = ff_add(rx, ff_neg(L[3 * j]));
     const ff dy = ff_add(ry, ff_neg(L[3 * j + 1]));
     const ff dz = ff_add(rz, ff_neg(L[3 * j + 2]));
     const ff rad = ff_add(ff_add(ff_sqr(dx), ff_sqr(dy)), ff_sqr(dz));
-    if (ff_lt(rad, sh.rh2ff[j]) && flags == 0) flags = (uint16_t)((sh.id[j] << 8) | 0x0001);
+    if (flags == 0) {
+        // rad.hi - rh2.hi is exact near the threshold (Sterbenz), so the FP32
+        // difference is good to a few units of the low parts
+        const float d = __fadd_rn(__fsub_rn(rad.hi, sh.rh2ff[j].hi), __fsub_rn(rad.lo, sh.rh2ff[j].lo));
+        border += fabsf(d) <= sh.rh2win[j] ? 1u : 0u;
+        if (ff_lt(rad, sh.rh2ff[j])) flags = (uint16_t)((sh.id[j] << 8) | 0x0001);
+    }
     const ff fac = pull_factor_ff(rad, sh.mff[j], sh.m15[j]);
     sx = ff_add(sx, ff_mul(dx, fac));
     sy = ff_add(sy, ff_mul(dy, fac));
     sz = ff_add(sz, ff_mul(dz, fac));
 }
 
+// The same kick term in FP64, as the reference computes it (src/wh.cu:142-160:
+// the FP64 squared distance compared with the FP64 rh^2, a -= m dr / |dr|^3
+// accumulated from a = h0), with |dr|^-3 from the FP64 reciprocal square root
+// (the reference's 1 / (rad sqrt(rad)) to rounding).  The build's FP64-kick
+// kernels use it (GLISSER_KICK_FP64).
+__device__ __forceinline__ void planet_kick64(const double* L, int j, double rx, double ry, double rz, double& ax,
+                                              double& ay, double& az, uint16_t& flags, uint32_t& border,
+                                              const CtaShared& sh)
+{
+    const double dx = rx - L[3 * j], dy = ry - L[3 * j + 1], dz = rz - L[3 * j + 2];
+    const double rad = fma(dx, dx, fma(dy, dy, dz * dz));
+    if (flags == 0) {
+        border += near_nonneg(rad, sh.rh2[j]);
+        if (lt_nonneg(rad, sh.rh2[j])) flags = (uint16_t)((sh.id[j] << 8) | 0x0001);
+    }
+    const double y = rsqrt_fast(rad);
+    const double fac = sh.m[j] * (y * (y * y));
+    ax = fma(-dx, fac, ax);
+    ay = fma(-dy, fac, ay);
+    az = fma(-dz, fac, az);
+}
+
 // Integrates particles first + k*CTA + tid (k < PPT, below first + count)
 // of one system over the block, staging that system's log through the two
 // buffers.  `phase` counts completed waits per buffer (identical in every
 // thread; carried across tiles of a persistent CTA).  Returns false after a
-// staging timeout.
-template <int NP, int CTA, int PPT, bool LEARNED>
+// staging timeout.  KICK64: the planet kick and its radius tests in FP64
+// (planet_kick64) instead of float-float.
+template <int NP, int CTA, int PPT, bool LEARNED, bool KICK64>
 __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uint32_t first, uint32_t count,
                                          double* stage, CtaShared& sh, uint32_t* phase)
 {
@@ -153,7 +199,7 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
     double rx[PPT], ry[PPT], rz[PPT], vx[PPT], vy[PPT], vz[PPT], ax[PPT], ay[PPT], az[PPT], r2[PPT], rinv[PPT];
     uint16_t flags[PPT], flags0[PPT];
     uint32_t dti[PPT];
-    uint32_t evals = 0;
+    uint32_t evals = 0, border = 0, nets = 0;
     const double hdt = p.dt * 0.5;
     const double mu = sh.m[0];
     const double rh2_sun = sh.rh2[0];
@@ -207,29 +253,50 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
         }
         const uint32_t cfirst = c * p.chunk;
         const uint32_t steps = min(p.chunk, p.len - cfirst);
-        // the chunk's planet log as float-floats, in place (each 8-byte double
-        // becomes the 8-byte pair of floats the kick reads)
         double* Lw = stage + b * bufstride;
-        for (uint32_t i = tid; i < steps * rec; i += CTA) reinterpret_cast<ff*>(Lw)[i] = ff_split(Lw[i]);
+        if constexpr (!KICK64) {
+            // the chunk's planet log as float-floats, in place (each 8-byte
+            // double becomes the 8-byte pair of floats the kick reads)
+            for (uint32_t i = tid; i < steps * rec; i += CTA) reinterpret_cast<ff*>(Lw)[i] = ff_split(Lw[i]);
+        }
         __syncthreads();
-        const ff* L0 = reinterpret_cast<const ff*>(Lw);
         for (uint32_t s = 0; s < steps; s++) {
-            const ff* L = L0 + (size_t)s * rec;
+            const ff* L = reinterpret_cast<const ff*>(Lw) + (size_t)s * rec;
+            const double* Ld = Lw + (size_t)s * rec;
 #pragma unroll
             for (int k = 0; k < PPT; k++) {
                 DriftInvariants q;
                 double guess = -1.0;
                 if constexpr (LEARNED) {
-                    // every lane, flagged or not: the network runs on the
-                    // warp's tensor cores (zero inputs for a lane without a drift)
-                    q = drift_invariants(rx[k], ry[k], rz[k], vx[k], vy[k], vz[k], r2[k], rinv[k], p.dt, mu);
-                    float x0 = 0.0f, x1 = 0.0f, x2 = 0.0f;
-                    const bool in_box =
-                        flags[k] == 0 && mlp_inputs(p.mlp, q.tau2, q.u, rinv[k], q.mu_r, q.alpha, x0, x1, x2);
-                    if (!in_box) x0 = x1 = x2 = 0.0f;
-                    __syncwarp();
-                    const float y = mlp_forward_warp(p.mlp, x0, x1, x2);
-                    if (in_box) guess = learned_guess(p.mlp, q.T, q.tau2, y);
+                    // The network runs where the series starter is outside its
+                    // domain (tau^2 >= SERIES_TAU2_MAX: a step that is a sizeable
+                    // part of the local dynamical time), in place of the FP32
+                    // pre-solve; elsewhere the series starter does.  It runs on
+                    // the warp's tensor cores, so the decision is warp-uniform:
+                    // all lanes evaluate it (zero inputs for a lane that does not
+                    // need it).  Every lane of the warp reaches this point on
+                    // every step and every k -- no lane may leave the step or
+                    // particle loops early while LEARNED is set, or the MMAs
+                    // below would run with part of the warp.
+                    bool want = false;
+                    if (flags[k] == 0) {
+                        q = drift_invariants(rx[k], ry[k], rz[k], vx[k], vy[k], vz[k], r2[k], rinv[k], p.dt, mu);
+                        want = !(q.tau2 < SERIES_TAU2_MAX);
+                    }
+                    if (__any_sync(0xffffffffu, want)) {
+                        float x0 = 0.0f, x1 = 0.0f, x2 = 0.0f;
+                        const bool in_box = want && mlp_inputs(p.mlp, q.tau2, q.u, rinv[k], q.mu_r, q.alpha, x0, x1, x2);
+                        if (!in_box) x0 = x1 = x2 = 0.0f;
+#ifdef GLISSER_MLP_INLINE
+                        const float y = mlp_forward_warp(p.mlp, x0, x1, x2);
+#else
+                        const float y = mlp_forward_warp_call(p.mlp, x0, x1, x2);
+#endif
+                        if (in_box) {
+                            guess = learned_guess(p.mlp, q.T, q.tau2, y);
+                            nets++;
+                        }
+                    }
                 }
                 if (flags[k] != 0) continue;
                 if constexpr (!LEARNED)
@@ -238,30 +305,35 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
                                                        p.dt, mu, p.starter, guess, p.tol_dt);
                 uint16_t fl = d.flags;
                 evals += d.evals;
-                const ff fx = ff_split(rx[k]), fy = ff_split(ry[k]), fz = ff_split(rz[k]);
-                ff sx = { 0.0f, 0.0f }, sy = { 0.0f, 0.0f }, sz = { 0.0f, 0.0f };
-                if constexpr (NP > 0) {
-#pragma unroll
-                    for (int j = 1; j <= NP; j++) planet_kick(L, j, fx, fy, fz, sx, sy, sz, fl, sh);
-                } else {
-                    for (int j = 1; j <= np; j++) planet_kick(L, j, fx, fy, fz, sx, sy, sz, fl, sh);
-                }
-                // a = h0 - sum of the planets' pulls
-                const ff gx = ff_add(L[0], ff_neg(sx)), gy = ff_add(L[1], ff_neg(sy)), gz = ff_add(L[2], ff_neg(sz));
-                // to FP64 on the integer pipe where the FP64 pipe is the bound; the
-                // learned kernel, bound by the network's FP32 work and issue,
-                // measured faster with the FP64 addition
                 double aax, aay, aaz;
-                if constexpr (LEARNED) {
-                    aax = f64_of_f32(gx.hi) + f64_of_f32(gx.lo);
-                    aay = f64_of_f32(gy.hi) + f64_of_f32(gy.lo);
-                    aaz = f64_of_f32(gz.hi) + f64_of_f32(gz.lo);
+                if constexpr (KICK64) {
+                    aax = Ld[0]; aay = Ld[1]; aaz = Ld[2];
+                    if constexpr (NP > 0) {
+#pragma unroll
+                        for (int j = 1; j <= NP; j++)
+                            planet_kick64(Ld, j, rx[k], ry[k], rz[k], aax, aay, aaz, fl, border, sh);
+                    } else {
+                        for (int j = 1; j <= np; j++)
+                            planet_kick64(Ld, j, rx[k], ry[k], rz[k], aax, aay, aaz, fl, border, sh);
+                    }
                 } else {
+                    const ff fx = ff_split(rx[k]), fy = ff_split(ry[k]), fz = ff_split(rz[k]);
+                    ff sx = { 0.0f, 0.0f }, sy = { 0.0f, 0.0f }, sz = { 0.0f, 0.0f };
+                    if constexpr (NP > 0) {
+#pragma unroll
+                        for (int j = 1; j <= NP; j++) planet_kick(L, j, fx, fy, fz, sx, sy, sz, fl, border, sh);
+                    } else {
+                        for (int j = 1; j <= np; j++) planet_kick(L, j, fx, fy, fz, sx, sy, sz, fl, border, sh);
+                    }
+                    // a = h0 - sum of the planets' pulls, to FP64 on the integer pipe
+                    const ff gx = ff_add(L[0], ff_neg(sx)), gy = ff_add(L[1], ff_neg(sy)),
+                             gz = ff_add(L[2], ff_neg(sz));
                     aax = ff_to_f64(gx);
                     aay = ff_to_f64(gy);
                     aaz = ff_to_f64(gz);
                 }
                 const double rr = r2[k];
+                border += near_nonneg(rr, rh2_sun) + near_nonneg(rr, p.outer2);
                 if (lt_nonneg(rr, rh2_sun)) fl = 0x0001;
                 if (gt_nonneg(rr, p.outer2)) fl = 0x0002;
                 flags[k] = fl;
@@ -292,7 +364,9 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
     for (int k = 0; k < PPT; k++) {
         const uint32_t off = (uint32_t)k * CTA + tid;
         const uint32_t i = first + off;
-        const bool active = off < count;
+        // a particle flagged before the block (the ensemble kernel's tiles keep
+        // removed particles in place) was not integrated: nothing to store
+        const bool active = off < count && flags0[k] == 0;
         if (active) {
             if (p.kill == GLISSER_ENCOUNTERS_KILL && (flags[k] & 0x01))
                 flags[k] = (uint16_t)((flags[k] & 0xFF00) | 0x80);
@@ -333,6 +407,20 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
         for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
         if (lane == 0 && e) atomicAdd(p.ho.evals, e);
     }
+    if (p.ho.borderline) {
+        unsigned long long e = border;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
+        if (lane == 0 && e) atomicAdd(p.ho.borderline, e);
+    }
+    if constexpr (LEARNED) {
+        if (p.ho.learned) {
+            unsigned long long e = nets;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
+            if (lane == 0 && e) atomicAdd(p.ho.learned, e);
+        }
+    }
     return ok;
 }
 
@@ -345,6 +433,7 @@ __device__ __forceinline__ void load_planet_constants(CtaShared& sh, uint32_t np
         sh.rh2[j] = rh[j] * rh[j];
         sh.mff[j] = ff_split(m[j]);
         sh.rh2ff[j] = ff_split(sh.rh2[j]);
+        sh.rh2win[j] = sh.rh2ff[j].hi * 0x1p-40f;
         sh.id[j] = pid[j];
     }
 }
@@ -371,6 +460,7 @@ inline bool fill_common(Common& p, const glisser_particles* pa, const glisser_st
     p.tol_dt = (sp->kepler_tol > 0 ? sp->kepler_tol : KEP_TOL) * sp->dt;
     p.starter = sp->starter;
     p.kill = sp->kill_encounters;
+    p.kick64 = sp->kick == GLISSER_KICK_FP64;
     p.mlp = reinterpret_cast<const MlpDev*>(sp->mlp);
     if (p.starter == STARTER_LEARNED && !p.mlp) p.starter = STARTER_SERIES;
     p.ho = *ho;

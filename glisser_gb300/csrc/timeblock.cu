@@ -61,6 +61,7 @@ int launch_timeblock(const glisser_particles* pa, size_t n_alive, const glisser_
     if (!(sp->kepler_tol == 0 || (sp->kepler_tol >= 1e-16 && sp->kepler_tol <= 1e-8))) return GLISSER_E_INVALID;
     if (sp->kill_encounters < GLISSER_ENCOUNTERS_KEEP || sp->kill_encounters > GLISSER_ENCOUNTERS_ROLLBACK)
         return GLISSER_E_INVALID;
+    if (sp->kick != GLISSER_KICK_FLOAT_FLOAT && sp->kick != GLISSER_KICK_FP64) return GLISSER_E_INVALID;
     if (pl->len > 0) {
         if (!pl->log || !pl->m || !pl->id || !pl->rh) return GLISSER_E_INVALID;
         if (((uintptr_t)pl->log & 15u) != 0) return GLISSER_E_INVALID;
@@ -73,22 +74,12 @@ int launch_timeblock(const glisser_particles* pa, size_t n_alive, const glisser_
     size_t smem = timeblock_smem_bytes(pl->npl, (int)p.chunk);
     uint32_t n = (uint32_t)n_alive;
     cudaError_t e;
-    if (sp->starter == GLISSER_STARTER_LEARNED && p.mlp) {
+    if (sp->starter == GLISSER_STARTER_LEARNED && p.mlp)
         e = launch_timeblock_learned(p, pl, n, smem, stream);
-    } else {
-        switch (pl->npl - 1) {
-        case 0: e = launch_np<0, false>(p, pl, n, smem, stream); break;
-        case 1: e = launch_np<1, false>(p, pl, n, smem, stream); break;
-        case 2: e = launch_np<2, false>(p, pl, n, smem, stream); break;
-        case 3: e = launch_np<3, false>(p, pl, n, smem, stream); break;
-        case 4: e = launch_np<4, false>(p, pl, n, smem, stream); break;
-        case 5: e = launch_np<5, false>(p, pl, n, smem, stream); break;
-        case 6: e = launch_np<6, false>(p, pl, n, smem, stream); break;
-        case 7: e = launch_np<7, false>(p, pl, n, smem, stream); break;
-        case 8: e = launch_np<8, false>(p, pl, n, smem, stream); break;
-        default: e = launch_np<0, false>(p, pl, n, smem, stream); break;
-        }
-    }
+    else if (p.kick64)
+        e = launch_timeblock_kick64(p, pl, n, smem, stream);
+    else
+        e = launch_variant<false, false>(p, pl, n, smem, stream);
     if (e != cudaSuccess) {
         snprintf(g_err, sizeof g_err, "time-block launch: %s", cudaGetErrorString(e));
         return GLISSER_E_CUDA;

@@ -18,12 +18,13 @@ using namespace tile;
 #define GLISSER_TB_MIN_BLOCKS 10
 #endif
 
-// The learned-starter kernel carries the network's layer-1 activations and
-// the hidden layer's accumulators on top of the drift's registers.  A bound
-// of 7 CTAs per SM (ptxas picks 128 registers, spilling 72 bytes) measured
-// within 1 % of 5, 6 and 8.
+// The learned-starter kernel runs the network only in a warp-uniform branch
+// taken where the series starter is outside its domain; it is held to the
+// plain kernel's occupancy, so that the registers the network needs on top
+// of the drift's are spilled around that branch instead of lowering the
+// occupancy of every step.
 #ifndef GLISSER_TB_MIN_BLOCKS_LEARNED
-#define GLISSER_TB_MIN_BLOCKS_LEARNED 7
+#define GLISSER_TB_MIN_BLOCKS_LEARNED GLISSER_TB_MIN_BLOCKS
 #endif
 
 // Particles per thread of the plain-starter kernel (a build-time tuning
@@ -34,7 +35,7 @@ using namespace tile;
 #define GLISSER_TB_PPT 1
 #endif
 
-template <int NP, bool LEARNED>
+template <int NP, bool LEARNED, bool KICK64>
 __global__ void __launch_bounds__(BLOCK_THREADS, LEARNED ? GLISSER_TB_MIN_BLOCKS_LEARNED : GLISSER_TB_MIN_BLOCKS)
     timeblock_kernel(const Common p, const double* log, const double* m, const double* rh, const uint32_t* pid,
                      uint32_t n)
@@ -47,14 +48,14 @@ __global__ void __launch_bounds__(BLOCK_THREADS, LEARNED ? GLISSER_TB_MIN_BLOCKS
     uint32_t phase[2] = { 0, 0 };
     constexpr int PPT = LEARNED ? 1 : GLISSER_TB_PPT;
     const uint32_t first = blockIdx.x * (uint32_t)(BLOCK_THREADS * PPT);
-    run_tile<NP, BLOCK_THREADS, PPT, LEARNED>(p, log, first, min((uint32_t)(BLOCK_THREADS * PPT), n - first), stage,
-                                              sh, phase);
+    run_tile<NP, BLOCK_THREADS, PPT, LEARNED, KICK64>(p, log, first, min((uint32_t)(BLOCK_THREADS * PPT), n - first),
+                                                      stage, sh, phase);
 }
 
-template <int NP, bool LEARNED>
+template <int NP, bool LEARNED, bool KICK64>
 cudaError_t launch_np(const Common& p, const glisser_planet_block* pl, uint32_t n, size_t smem, cudaStream_t stream)
 {
-    auto kern = timeblock_kernel<NP, LEARNED>;
+    auto kern = timeblock_kernel<NP, LEARNED, KICK64>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const uint32_t per_cta = (uint32_t)BLOCK_THREADS * (LEARNED ? 1u : (uint32_t)GLISSER_TB_PPT);
@@ -63,9 +64,43 @@ cudaError_t launch_np(const Common& p, const glisser_planet_block* pl, uint32_t 
     return cudaGetLastError();
 }
 
+// Dispatch over the planet count for one kernel variant.
+template <bool LEARNED, bool KICK64>
+cudaError_t launch_variant(const Common& p, const glisser_planet_block* pl, uint32_t n, size_t smem,
+                           cudaStream_t stream)
+{
+    if constexpr (LEARNED) {
+        // learned instantiations: one and four planets besides the Sun
+        // specialised, other counts on the generic planet loop
+        switch (pl->npl - 1) {
+        case 1: return launch_np<1, true, KICK64>(p, pl, n, smem, stream);
+        case 4: return launch_np<4, true, KICK64>(p, pl, n, smem, stream);
+        default: return launch_np<0, true, KICK64>(p, pl, n, smem, stream);
+        }
+    } else {
+        switch (pl->npl - 1) {
+        case 1: return launch_np<1, false, KICK64>(p, pl, n, smem, stream);
+        case 2: return launch_np<2, false, KICK64>(p, pl, n, smem, stream);
+        case 3: return launch_np<3, false, KICK64>(p, pl, n, smem, stream);
+        case 4: return launch_np<4, false, KICK64>(p, pl, n, smem, stream);
+        case 5: return launch_np<5, false, KICK64>(p, pl, n, smem, stream);
+        case 6: return launch_np<6, false, KICK64>(p, pl, n, smem, stream);
+        case 7: return launch_np<7, false, KICK64>(p, pl, n, smem, stream);
+        case 8: return launch_np<8, false, KICK64>(p, pl, n, smem, stream);
+        default: return launch_np<0, false, KICK64>(p, pl, n, smem, stream);
+        }
+    }
+}
+
 }  // namespace
 
-// Learned-starter launch (timeblock_learned.cu).
+// Launches of the variants compiled in other translation units (each unit
+// instantiates one variant, so that the units compile in parallel and keep
+// their register allocations apart): plain starters with the FP64 kick
+// (timeblock_kick64.cu), the learned starter with either kick
+// (timeblock_learned.cu).
+cudaError_t launch_timeblock_kick64(const tile::Common& p, const glisser_planet_block* pl, uint32_t n, size_t smem,
+                                    cudaStream_t stream);
 cudaError_t launch_timeblock_learned(const tile::Common& p, const glisser_planet_block* pl, uint32_t n, size_t smem,
                                      cudaStream_t stream);
 

@@ -20,6 +20,10 @@ from . import (F32, SZ, MlpNorm, ParticlesDev, _p, _raise, last_error, lib, STAR
                STARTER_LEARNED)
 
 NPARAM = 1217
+# tau^2 = dt^2 mu / r0^3 from which the kernels run the network instead of the
+# series starter, and the log floor that trains it with a margin below
+SERIES_TAU2_MAX = 0.01
+LOG_TAU2_FLOOR = 0.005
 OFF_W1, OFF_B1, OFF_W2, OFF_B2, OFF_W3, OFF_B3 = 0, 96, 128, 1152, 1184, 1216
 
 
@@ -59,6 +63,11 @@ class Trainer:
         n = C.c_size_t()
         _check(lib().glisser_mlp_log_simulation(self.h, sim.h, C.byref(n)))
         return n.value
+
+    def set_log_floor(self, tau2_min):
+        """Keep only logged drifts with tau^2 >= tau2_min (the kernels run the
+        network where tau^2 >= SERIES_TAU2_MAX)."""
+        _check(lib().glisser_mlp_set_log_floor(self.h, tau2_min))
 
     def add_samples(self, feat, target):
         feat = np.ascontiguousarray(feat, np.float32)
@@ -144,6 +153,17 @@ class Trainer:
         d = C.c_void_p()
         _check(lib().glisser_mlp_device_weights(self.h, C.byref(d)))
         return d.value
+
+
+def pack(params):
+    """The inference routine's tensor-core B operands for the flattened
+    parameters: (w1p [32, 4], w2p [32, 16]) uint32 BF16 pairs."""
+    from . import U32
+    p = np.ascontiguousarray(params, np.float32)
+    w1p = np.zeros((32, 4), np.uint32)
+    w2p = np.zeros((32, 16), np.uint32)
+    _check(lib().glisser_mlp_pack(_p(p, F32), _p(w1p, U32), _p(w2p, U32)))
+    return w1p, w2p
 
 
 def drift_states(r, v, dt, mu, starter=STARTER_SERIES, trainer=None):

@@ -80,9 +80,29 @@ def build(verbose=False):
         if r.returncode != 0:
             raise RuntimeError("link failed: %s\n%s" % (r.stdout, r.stderr))
         os.replace(tmp, LIB)
+    build_cli()
     if verbose:
         print("built", LIB)
     return LIB
+
+
+CLI_SRC = os.path.join(HERE, "cli", "glisser_main.cpp")
+CLI = os.path.join(OUT, "glisser")
+
+
+def build_cli():
+    """The glisser command (cli/glisser_main.cpp) linked against the library,
+    which it finds next to itself."""
+    if os.path.exists(CLI) and os.path.getmtime(CLI) >= max(os.path.getmtime(CLI_SRC), os.path.getmtime(LIB)):
+        return CLI
+    tmp = CLI + ".tmp%d" % os.getpid()
+    cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-Wextra", "-I" + os.path.join(ROOT, "include"), CLI_SRC, "-o", tmp,
+           "-L" + OUT, "-lglisser_gb300", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("glisser command build failed: %s\n%s" % (r.stdout, r.stderr))
+    os.replace(tmp, CLI)
+    return CLI
 
 
 if __name__ == "__main__":

@@ -1,6 +1,9 @@
 """Seeded synthetic workloads (orbital elements; angles in radians): the five
 benchmark workloads, named for what they are -- plain-neptune, plain-giants,
-scattered-disk, ensembles, history-encounters.
+scattered-disk, ensembles, history-encounters -- and close-eccentric, the
+regime of the scattered disk's pericentre passages on its own (every drift a
+sizeable part of the local dynamical time, tau^2 = dt^2 mu / r^3 > 0.01, where
+the series starter does not apply and the learned starter runs its network).
 
 The reference ships no particle state for its examples (the 200,000-particle
 resonance state is not distributed), so every workload here is generated:
@@ -66,6 +69,9 @@ WORKLOADS = {
                       cull=0.5, outer=300.0, planets="giants", a=(40, 50), e=(0, 0.1), i=5.0),
     "history-encounters": dict(n=2_000_000, dt=0.2, steps=50_000, tbsize=100, cull=0.5, outer=300.0,
                                planets="neptune-yr", a=(20, 40), e=(0, 0.3), i=10.0, esf=3.0, hist_every=100),
+    # r = a (1 +- e) within 1.0 .. 9.6 au: tau^2 >= 0.0108 at dt = 180 d
+    "close-eccentric": dict(n=1_000_000, dt=180.0, steps=10_000, tbsize=512, cull=0.5, outer=1e5,
+                            planets="neptune", a=(2.5, 6.0), e=(0.1, 0.6), i=20.0),
 }
 
 

@@ -49,7 +49,7 @@ extern "C" {
 /* Kepler starters for the universal-variable drift. */
 #define GLISSER_STARTER_CLASSIC 0  /* the reference's kepu_guess, src/wh.cpp:188-220 */
 #define GLISSER_STARTER_SERIES 1   /* tenth-order time series / FP32 Kepler pre-solve */
-#define GLISSER_STARTER_LEARNED 2  /* MLP initial guess, classic fallback */
+#define GLISSER_STARTER_LEARNED 2  /* series where it applies, else the MLP initial guess; classic fallback */
 
 /* What the time-block kernel does with a particle that ends the block in a
  * close encounter (flags != 0, (flags & 0xFE) == 0), glisser_step_params
@@ -58,6 +58,11 @@ extern "C" {
 #define GLISSER_ENCOUNTERS_KILL 1      /* 0x01 -> 0x80 (KillEncounterKernel, src/executor.cu:63-77) */
 #define GLISSER_ENCOUNTERS_ROLLBACK 2  /* keeps the flag and its block-start r, v: the rollback state the
                                           SWIFT hand-off resumes from (src/executor.cu:624-633, 827-834) */
+
+/* Arithmetic of the planet kick and its radius tests (glisser_step_params
+ * .kick).  The reference computes them in FP64 (src/wh.cu:142-172). */
+#define GLISSER_KICK_FLOAT_FLOAT 0  /* default: float-float (~48 bits) on the FP32 pipe; the drift stays FP64 */
+#define GLISSER_KICK_FP64 1         /* FP64, the reference's formulation */
 
 /* Feature normalisation and training box of a learned starter (features
  * f0 = log(tau), tau = dt sqrt(mu/r0^3), f1 = r0.v0 / sqrt(mu r0),
@@ -108,6 +113,8 @@ typedef struct glisser_step_params {
     int32_t kill_encounters;     /* GLISSER_ENCOUNTERS_*: what a particle flagged 0x01 keeps */
     const void *mlp;             /* learned-starter weights (device), or NULL */
     double kepler_tol;           /* Kepler residual tolerance |f| < tol*dt; 0 = 1e-13 (the reference's DANBYB) */
+    int32_t kick;                /* GLISSER_KICK_*: arithmetic of the planet kick and its radius tests */
+    int32_t reserved;
 } glisser_step_params;
 
 /* Hand-off of the particles flagged during a block, compacted by warp ballot
@@ -115,7 +122,13 @@ typedef struct glisser_step_params {
  * `count` must be zeroed by the caller before the launch; on return it holds
  * the number of newly flagged particles (entries beyond `capacity` are
  * counted but not written).  `status` is ORed with GLISSER_STATUS_* bits.
- * `evals` (optional) accumulates the Stumpff evaluations spent. */
+ * `evals` (optional) accumulates the Stumpff evaluations spent.
+ * `borderline` (optional) accumulates the threshold-borderline radius tests:
+ * Hill-radius tests whose outcome counted and Sun / outer-limit tests whose
+ * squared distance lay within about 2^-40 (9e-13) of the squared radius, where
+ * two correct evaluations that round differently could flag differently.
+ * `learned` (optional) accumulates the drifts started from the learned
+ * starter's network guess. */
 typedef struct glisser_handoff {
     uint32_t *count;
     uint32_t *index;             /* position in the particle arrays */
@@ -126,6 +139,8 @@ typedef struct glisser_handoff {
     uint32_t reserved;
     uint32_t *status;
     unsigned long long *evals;
+    unsigned long long *borderline;
+    unsigned long long *learned;
 } glisser_handoff;
 
 #define GLISSER_STATUS_LOG_TIMEOUT 0x1u   /* planet-log staging wait gave up */
@@ -159,7 +174,9 @@ int glisser_partition(const glisser_particles *in, const glisser_particles *out,
  *   - n may not exceed glisser_partition_noalloc_max_particles() (8,388,608);
  *     larger n returns GLISSER_E_INVALID and launches nothing.
  *   - The first call on a device looks up the array's device address; make
- *     that first call before any stream capture.
+ *     that first call before any stream capture.  The address is kept with
+ *     the context it was looked up in and looked up again (on that call) when
+ *     the current context differs, as after a cudaDeviceReset.
  *   - All calls share the array and leave their counts in it; calls whose
  *     work overlaps on the GPU race and corrupt each other's result. */
 size_t glisser_partition_noalloc_max_particles(void);
@@ -203,6 +220,11 @@ int glisser_set_device_interp(glisser_t *h, int on);
  * accepted Newton correction is folded into the G-functions, so the solution
  * error is O(tol^2). */
 int glisser_set_kepler_tolerance(glisser_t *h, double tol);
+
+/* Arithmetic of the planet kick and its radius tests: GLISSER_KICK_FLOAT_FLOAT
+ * (the default) or GLISSER_KICK_FP64 (the reference's, src/wh.cu:142-172).
+ * May change between blocks. */
+int glisser_set_kick(glisser_t *h, int kick);
 
 /* Track snapshots (glisser_write_track) with the particle records built on
  * the device -- elements, float32 packing and id order in kernels, one
@@ -295,7 +317,9 @@ int glisser_swift_stats_get(const glisser_swift_stats *s, uint32_t id, int32_t *
 int glisser_swift_write_stat(const glisser_swift_stats *s, const char *path);
 
 /* Selects the Kepler starter (default GLISSER_STARTER_SERIES) and, for the
- * learned starter, the weights blob written by glisser_mlp_save. */
+ * learned starter, the weights blob written by glisser_mlp_save.  The learned
+ * starter takes the series starter where it applies (tau^2 = dt^2 mu / r0^3
+ * below 0.01) and the network's guess elsewhere inside its training box. */
 int glisser_set_starter(glisser_t *h, int starter, const char *mlp_path);
 
 /* Running totals since init: particle-steps integrated (each particle counts
@@ -303,6 +327,13 @@ int glisser_set_starter(glisser_t *h, int starter, const char *mlp_path);
  * evaluations spent by the Kepler solver.  No reference counterpart; the
  * reference reports timings only (timing.out, src/executor.cu:739-759). */
 int glisser_stats(const glisser_t *h, unsigned long long *particle_steps, unsigned long long *kepler_evals);
+/* Threshold-borderline radius tests since init (glisser_handoff.borderline):
+ * flag tests decided within about 2^-40 of their radius.  No reference
+ * counterpart; zero means no flag of the run depended on rounding. */
+int glisser_borderline(const glisser_t *h, unsigned long long *tests);
+/* Drifts started from the learned starter's network guess since init (the
+ * rest of a learned run took the series rule).  No reference counterpart. */
+int glisser_learned_drifts(const glisser_t *h, unsigned long long *drifts);
 /* Kernel launches issued by the executor since init, and its CUDA stream
  * (a cudaStream_t; the blocks' kernels and copies run on it). */
 int glisser_launches(const glisser_t *h, unsigned long long *launches);
@@ -333,6 +364,12 @@ int glisser_ensemble_set_starter(glisser_ensemble_t *e, int starter, const char 
  * before glisser_ensemble_init. */
 int glisser_ensemble_set_device_planets(glisser_ensemble_t *e, int on);
 int glisser_ensemble_set_kepler_tolerance(glisser_ensemble_t *e, double tol);
+/* GLISSER_KICK_* for every system (as glisser_set_kick). */
+int glisser_ensemble_set_kick(glisser_ensemble_t *e, int kick);
+/* Threshold-borderline radius tests since init (as glisser_borderline). */
+int glisser_ensemble_borderline(const glisser_ensemble_t *e, unsigned long long *tests);
+/* Drifts started from the network guess since init (as glisser_learned_drifts). */
+int glisser_ensemble_learned_drifts(const glisser_ensemble_t *e, unsigned long long *drifts);
 /* Planets of system s at the particles' time: m[npl], r/v[npl][3]
  * (heliocentric); *n receives npl, cap is the room in m / r / v. */
 int glisser_ensemble_get_planets(glisser_ensemble_t *e, size_t s, double *m, double *r, double *v, size_t cap,
@@ -342,6 +379,23 @@ int glisser_ensemble_step(glisser_ensemble_t *e, double *gpu_ms);
 int glisser_ensemble_counts(const glisser_ensemble_t *e, size_t s, size_t *n, size_t *n_alive);
 int glisser_ensemble_get_particles(glisser_ensemble_t *e, size_t s, double *r, double *v, uint32_t *id,
                                    uint16_t *flags, size_t cap, size_t *n);
+/* Every particle of every system at once, in system order ([n][3]
+ * heliocentric; n = the ensemble's total particle count), through pinned
+ * staging on the ensemble's stream: set_state replaces the positions and
+ * velocities the next block integrates (accelerations, flags and death
+ * records stay), get_state reads them (and the flags) back; it waits for the
+ * blocks in flight.  With r, v and flags all NULL get_state only reports *n.
+ * For a host that keeps the state in its own buffers between blocks. */
+int glisser_ensemble_set_state(glisser_ensemble_t *e, size_t n, const double *r, const double *v);
+int glisser_ensemble_get_state(glisser_ensemble_t *e, double *r, double *v, uint16_t *flags, size_t cap, size_t *n);
+/* The ensemble's CUDA stream (a cudaStream_t; its blocks run on it). */
+int glisser_ensemble_stream(const glisser_ensemble_t *e, void **stream);
+/* When each particle of system s (in id order) was flagged: deathtime = the
+ * end of that block as a float (as the executor stamps it, src/executor.cu
+ * resync2), deathtime_index = the step within the block; 0 for particles never
+ * flagged.  Arrays may be NULL; *n receives the particle count. */
+int glisser_ensemble_get_deaths(const glisser_ensemble_t *e, size_t s, double *deathtime, uint32_t *deathtime_index,
+                                size_t cap, size_t *n);
 int glisser_ensemble_stats(const glisser_ensemble_t *e, unsigned long long *particle_steps,
                            unsigned long long *kepler_evals, unsigned long long *launches);
 int glisser_ensemble_time(const glisser_ensemble_t *e, double *t);
@@ -404,6 +458,11 @@ int glisser_mlp_log_simulation(glisser_mlp_t *m, glisser_t *h, size_t *n_logged)
 /* The same for device states [0, n) (kernel layer; r and v are read). */
 int glisser_mlp_log_states(glisser_mlp_t *m, const glisser_particles *pa, size_t n, double dt, double mu,
                            void *stream, size_t *n_logged);
+/* Keeps only the logged drifts with tau^2 = dt^2 mu / r0^3 >= tau2_min (0, the
+ * default: all).  The time-block kernels run the network only where the
+ * series starter is outside its domain (tau^2 >= 0.01), so a network is
+ * trained on that range (with a margin below it). */
+int glisser_mlp_set_log_floor(glisser_mlp_t *m, double tau2_min);
 /* Host samples: feat[n][3], target[n] (z; NaN marks a sample to skip). */
 int glisser_mlp_add_samples(glisser_mlp_t *m, const float *feat, const float *target, size_t n);
 int glisser_mlp_get_samples(const glisser_mlp_t *m, float *feat, float *target, size_t first, size_t n);
@@ -432,6 +491,11 @@ int glisser_mlp_gradients(glisser_mlp_t *m, const float *feat, const float *targ
 int glisser_mlp_predict(glisser_mlp_t *m, const float *feat, size_t n, float *y);
 /* Weights file for glisser_set_starter / glisser_ensemble_set_starter. */
 int glisser_mlp_save(const glisser_mlp_t *m, const char *path);
+/* The tensor-core operands of the drift's inference for the flattened
+ * parameters (host memory, no device needed): W1 as the layer-1 MMA's B
+ * operand w1p [32][4] and W2 as the hidden layer's w2p [32][16], BF16 pairs
+ * with the lower index in the low half.  For checking the packing. */
+int glisser_mlp_pack(const float *params, uint32_t *w1p, uint32_t *w2p);
 /* The current weights as the drift reads them (device pointer owned by m,
  * valid until the next change of weights or normalisation). */
 int glisser_mlp_device_weights(glisser_mlp_t *m, const void **dev);

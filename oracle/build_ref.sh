@@ -1,9 +1,10 @@
 #!/usr/bin/env bash
-# Test infrastructure: compiles the UNMODIFIED reference sources where they lie
-# (default /root/reference, override with GLISSER_REF_DIR) together with
-# oracle/ref_driver.cu into oracle/_ref/libglisser_ref.so.  Only this
-# container has the reference tree; the library pins the oracle restatement and
-# generates tests/golden/.  It is never shipped or linked by the product.
+# Test infrastructure: compiles the UNMODIFIED reference sources -- the staged
+# copy in baseline/_ref/src (baseline/stage_ref.sh), or else the src/ directory
+# of the reference checkout named by GLISSER_REF_DIR -- together with
+# oracle/ref_driver.cu into oracle/_ref/libglisser_ref.so.  The library pins
+# the oracle restatement, generates tests/golden/ and is the reference CPU
+# baseline of bench.py; it is never shipped or linked by the product.
 #
 # The forced includes stand in for standard headers that the reference relies
 # on transitively and that GCC 13 no longer pulls in.  C++11 for the .cpp files
@@ -11,11 +12,14 @@
 # -ffp-contract=off keeps the host arithmetic free of fused multiply-adds so
 # that x86 and aarch64 builds of the oracle agree bit for bit.
 set -euo pipefail
-REF="${GLISSER_REF_DIR:-/root/reference}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
-if [ ! -f "$REF/src/wh.cu" ]; then
-    echo "reference sources not found at $REF" >&2
+SRC="$HERE/../baseline/_ref/src"
+if [ ! -f "$SRC/wh.cu" ]; then
+    SRC="${GLISSER_REF_DIR:?no staged reference sources: run baseline/stage_ref.sh or set GLISSER_REF_DIR}/src"
+fi
+if [ ! -f "$SRC/wh.cu" ]; then
+    echo "reference sources not found at $SRC" >&2
     exit 2
 fi
 mkdir -p "$OUT"
@@ -23,10 +27,10 @@ INCS="-include limits -include string -include cstring -include array -include m
 FLAGS="-O2 -fPIC -ffp-contract=off -DNO_CUDA -w"
 pids=()
 for f in wh convert data interp util swift; do
-    g++ -std=c++11 $FLAGS $INCS -c "$REF/src/$f.cpp" -o "$OUT/$f.o" &
+    g++ -std=c++11 $FLAGS $INCS -c "$SRC/$f.cpp" -o "$OUT/$f.o" &
     pids+=($!)
 done
-nvcc -std=c++17 -O2 -Xcompiler "-fPIC -ffp-contract=off -w" -I"$REF/src" $INCS \
+nvcc -std=c++17 -O2 -w -Xcompiler "-fPIC -ffp-contract=off -w" -I"$SRC" $INCS \
     -c "$HERE/ref_driver.cu" -o "$OUT/ref_driver.o" &
 pids+=($!)
 for p in "${pids[@]}"; do wait "$p"; done

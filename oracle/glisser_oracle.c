@@ -470,6 +470,18 @@ void orc_from_elements_M(double mu, double a, double e, double i, double capom, 
 	orc_from_elements(mu, a, e, i, capom, om, f, r, v);
 }
 
+/* orc_from_elements_M over n element rows (a, e, i, capom, om, M) into [n][3]
+ * r and v: the particle generator of targets/make_state.cpp:126-165 without its
+ * RNG, for callers that must not load the product library. */
+void orc_elements_to_cartesian(size_t n, double mu, const double* el, double* r, double* v)
+{
+	for (size_t k = 0; k < n; k++)
+	{
+		const double* e = el + 6 * k;
+		orc_from_elements_M(mu, e[0], e[1], e[2], e[3], e[4], e[5], r + 3 * k, v + 3 * k);
+	}
+}
+
 /* src/convert.cpp:337-490; out6 = a, e, i, capom, om, f */
 void orc_to_elements(double mu, const double* rr_, const double* vv_, int* esignout, double* out6)
 {

@@ -53,6 +53,7 @@ def lib():
         L.orc_uv_drift.argtypes = [C.c_size_t, D, D, U16, C.c_double, C.c_double, I32]
         L.orc_from_elements_M.argtypes = [C.c_double] * 7 + [D, D]
         L.orc_from_elements.argtypes = [C.c_double] * 7 + [D, D]
+        L.orc_elements_to_cartesian.argtypes = [C.c_size_t, C.c_double, D, D, D]
         L.orc_to_elements.argtypes = [C.c_double, D, D, I32, D]
         L.orc_mean_anomaly.argtypes = [C.c_double, C.c_double]
         L.orc_mean_anomaly.restype = C.c_double
@@ -78,6 +79,40 @@ def lib():
 
 def _p(a, t):
     return a.ctypes.data_as(t)
+
+
+REF_LIB = os.path.join(HERE, "_ref", "libglisser_ref.so")
+_ref = None
+
+
+def reference_lib():
+    """The reference's own CPU build (oracle/build_ref.sh from the staged
+    sources), or None where it was not built."""
+    global _ref
+    if _ref is None and os.path.exists(REF_LIB):
+        L = C.CDLL(REF_LIB)
+        L.ref_mvs_block.argtypes = [C.c_size_t, D, D, D, U16, U32, C.c_uint32, C.c_uint32, D, D, D, U32, D,
+                                    C.c_double, C.c_double, C.c_double]
+        L.ref_mvs_block.restype = None
+        _ref = L
+    return _ref
+
+
+def reference_block(r, v, a, flags, tbsize, npl, h0_log, r_log, m, pl_id, rh, outer_r, dt, mu):
+    """One time block of the reference's own MVSKernel::step_forward
+    (src/wh.cu:113-177), compiled for the host, over [n, 3] arrays r, v, a
+    (updated in place); returns (flags, deathtime_index)."""
+    L = reference_lib()
+    if L is None:
+        raise RuntimeError("the reference's CPU build is missing (oracle/build_ref.sh)")
+    n = r.shape[0]
+    flags = np.ascontiguousarray(flags, dtype=np.uint16).copy()
+    dti = np.zeros(n, np.uint32)
+    L.ref_mvs_block(n, _p(r, D), _p(v, D), _p(a, D), _p(flags, U16), _p(dti, U32), tbsize, npl,
+                    _p(np.ascontiguousarray(h0_log, np.float64), D), _p(np.ascontiguousarray(r_log, np.float64), D),
+                    _p(np.ascontiguousarray(m, np.float64), D), _p(np.ascontiguousarray(pl_id, np.uint32), U32),
+                    _p(np.ascontiguousarray(rh, np.float64), D), outer_r, dt, mu)
+    return flags, dti
 
 
 def block(r, v, a, flags, tbsize, npl, h0_log, r_log, m, pl_id, rh, outer_r, dt, mu, drift="mvs"):
@@ -115,6 +150,16 @@ def from_elements_M(mu, a, e, i, capom, om, M):
     r = np.zeros(3)
     v = np.zeros(3)
     lib().orc_from_elements_M(mu, a, e, i, capom, om, M, _p(r, D), _p(v, D))
+    return r, v
+
+
+def elements_to_cartesian(mu, el):
+    """[n, 6] elements (a, e, i, capom, om, M) -> r, v [n, 3] by the
+    oracle's from_elements_M (src/convert.cpp:257-275)."""
+    el = np.ascontiguousarray(el, np.float64)
+    r = np.zeros((len(el), 3))
+    v = np.zeros((len(el), 3))
+    lib().orc_elements_to_cartesian(len(el), mu, _p(el, D), _p(r, D), _p(v, D))
     return r, v
 
 

@@ -1,8 +1,8 @@
 """Generates the golden fixtures in tests/golden/ by running the UNMODIFIED
 reference sources (compiled by oracle/build_ref.sh into oracle/_ref/).
 
-Run in a container that has the reference tree:
-    python tests/golden/make_golden.py
+Run where the reference checkout is available:
+    GLISSER_REF_DIR=<reference checkout> python tests/golden/make_golden.py
 Only this script reads the reference; the fixtures it writes are what the
 tests (here and on the GPU host) compare against.
 """
@@ -21,7 +21,9 @@ from glisser_gb300 import synth  # noqa: E402
 from glisser_gb300.metrics import jacobi_constant  # noqa: E402
 
 REF_LIB = os.path.join(ROOT, "oracle", "_ref", "libglisser_ref.so")
-REFERENCE = os.environ.get("GLISSER_REF_DIR", "/root/reference")
+REFERENCE = os.environ.get("GLISSER_REF_DIR")
+if not REFERENCE:
+    sys.exit("make_golden.py: set GLISSER_REF_DIR to the reference checkout")
 D = C.POINTER(C.c_double)
 U32 = C.POINTER(C.c_uint32)
 U16 = C.POINTER(C.c_uint16)

@@ -50,14 +50,15 @@ class DevHandoff:
     def __init__(self, capacity):
         dev = torch.device("cuda:0")
         self.ctr = torch.zeros(4, dtype=torch.int32, device=dev)
-        self.evals = torch.zeros(1, dtype=torch.int64, device=dev)
+        self.evals = torch.zeros(3, dtype=torch.int64, device=dev)
         self.index = torch.zeros(max(capacity, 1), dtype=torch.int32, device=dev)
         self.ids = torch.zeros(max(capacity, 1), dtype=torch.int32, device=dev)
         self.flags = torch.zeros(max(capacity, 1), dtype=torch.int16, device=dev)
         self.dti = torch.zeros(max(capacity, 1), dtype=torch.int32, device=dev)
         self.view = G.HandoffDev(self.ctr.data_ptr(), self.index.data_ptr(), self.ids.data_ptr(),
                                  self.flags.data_ptr(), self.dti.data_ptr(), capacity, 0,
-                                 self.ctr.data_ptr() + 4, self.evals.data_ptr())
+                                 self.ctr.data_ptr() + 4, self.evals.data_ptr(), self.evals.data_ptr() + 8,
+                                 self.evals.data_ptr() + 16)
 
     def reset(self):
         self.ctr.zero_()
@@ -67,17 +68,19 @@ class DevHandoff:
         torch.cuda.synchronize()
         c = self.ctr.cpu().numpy()
         k = int(c[0])
-        return dict(count=k, status=int(c[1]), evals=int(self.evals.cpu().numpy()[0]),
+        ev = self.evals.cpu().numpy()
+        return dict(count=k, status=int(c[1]), evals=int(ev[0]), borderline=int(ev[1]), learned=int(ev[2]),
                     index=self.index[:k].cpu().numpy().view(np.uint32), id=self.ids[:k].cpu().numpy().view(np.uint32),
                     flags=self.flags[:k].cpu().numpy().view(np.uint16), dti=self.dti[:k].cpu().numpy().view(np.uint32))
 
 
-def timeblock(parts, blk, dt, outer, starter=G.STARTER_SERIES, kill=True, handoff=None, mlp=0, encounters=None):
+def timeblock(parts, blk, dt, outer, starter=G.STARTER_SERIES, kill=True, handoff=None, mlp=0, encounters=None,
+              kick=G.KICK_FLOAT_FLOAT):
     """One block through the C ABI; `encounters` (G.ENCOUNTERS_*) overrides `kill`."""
     ho = handoff or DevHandoff(parts.n)
     ho.reset()
     mode = (G.ENCOUNTERS_KILL if kill else G.ENCOUNTERS_KEEP) if encounters is None else encounters
-    sp = G.StepParams(dt, outer, starter, mode, mlp)
+    sp = G.StepParams(dt, outer, starter, mode, mlp, 0.0, kick)
     G.integrate_timeblock(parts.view, parts.n, blk.view, sp, ho.view)
     return ho.result()
 

@@ -22,15 +22,28 @@ def test_algorithmic_flops_convention():
     assert bench.alg_flops_per_particle_step(4, k_ref=3) == 213
 
 
-def test_executed_fp64_view():
-    v = bench.executed_fp64_view(4, 1e10, 1.25)
-    c = bench.FP64_INSTR_PER_STEP_NP4
+@pytest.mark.parametrize("kernel", sorted(bench.FP64_COUNTS))
+def test_executed_fp64_view(kernel):
+    v = bench.executed_fp64(kernel, 1e10, 1.25)
+    c = bench.FP64_COUNTS[kernel]
     flops = c["dadd"] + c["dmul"] + 2 * c["dfma"]
     assert v["flops_per_particle_step"] == pytest.approx(flops)
     assert v["achieved"] == pytest.approx(1e10 * flops / 1e12)
     assert v["frac"] == pytest.approx(v["achieved"] / 1.25)
     assert 0 < v["fp64_pipe_busy"] <= 1
-    assert bench.executed_fp64_view(1, 1e10, 1.25) is None     # counted for the 4-planet kernel only
+    assert os.path.exists(os.path.join(ROOT, c["profile"]))
+    assert bench.executed_fp64("no such kernel", 1e10, 1.25) is None
+
+
+def test_reference_arm_does_not_load_the_library():
+    """The reference arm times the reference's CPU code on inputs the oracle
+    makes: this library's shared object is never mapped."""
+    code = ("import sys, runpy; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '0', "
+            "'--sample-particles', '256', '--sample-steps', '8']; runpy.run_path('bench.py', run_name='__main__'); "
+            "maps = open('/proc/self/maps').read(); print('LOADED' if 'libglisser_gb300' in maps else 'CLEAN')")
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert out.stdout.strip().splitlines()[-1] == "CLEAN"
 
 
 def test_reference_arm_prints_one_contract_line():

@@ -56,9 +56,13 @@ def by_id(p):
 
 
 @pytest.mark.parametrize("case", CASES)
-@pytest.mark.parametrize("starter", [G.STARTER_SERIES, G.STARTER_CLASSIC])
-def test_kernel_block_parity(case, starter):
-    """The C-ABI time-block kernel, block after block, against the oracle."""
+@pytest.mark.parametrize("starter,kick", [(G.STARTER_SERIES, G.KICK_FLOAT_FLOAT), (G.STARTER_CLASSIC, G.KICK_FLOAT_FLOAT),
+                                          (G.STARTER_SERIES, G.KICK_FP64)])
+def test_kernel_block_parity(case, starter, kick):
+    """The C-ABI time-block kernel, block after block, against the oracle,
+    with the float-float kick and with the FP64 kick.  No radius test of
+    these fixtures is threshold-borderline (glisser_handoff.borderline), so
+    the flags cannot depend on the kick's arithmetic."""
     from gpu_util import DevParticles, DevPlanetBlock, DevHandoff, timeblock, rel_err
     d, cfg = load(case)
     ex = oracle_exec(d, cfg)
@@ -72,8 +76,9 @@ def test_kernel_block_parity(case, starter):
         c = ex.counts()
         dev_blk = DevPlanetBlock(blk["h0_log"], blk["r_log"], blk["m"], blk["id"], blk["rh"])
         before = by_id(parts.host())["flags"].copy()
-        res = timeblock(parts, dev_blk, c["dt"], outer, starter=starter, handoff=ho)
+        res = timeblock(parts, dev_blk, c["dt"], outer, starter=starter, handoff=ho, kick=kick)
         assert res["status"] == 0
+        assert res["borderline"] == 0, b
         ex.loop()
         steps += blk["log_len"]
         got = by_id(parts.host())
@@ -87,6 +92,36 @@ def test_kernel_block_parity(case, starter):
         assert err.max() < POS_TOL * max(1.0, steps / 1000.0), (b, err.max())
         verr = rel_err(got["v"], want["v"])
         assert verr.max() < POS_TOL * max(1.0, steps / 1000.0), (b, verr.max())
+
+
+@pytest.mark.parametrize("kick", [G.KICK_FLOAT_FLOAT, G.KICK_FP64])
+def test_plain_giants_against_oracle_both_kicks(kick):
+    """The plain-giants workload (Sun + four giants, particles near the
+    Neptune 3:1, a 53-57 au, e < 0.3, i < 10 deg; dt = 180 d) on a 4,096-
+    particle sample over 1,024 steps through the executor, with each kick:
+    flags and survivors equal to the oracle's, positions within 1e-10
+    relative, no threshold-borderline radius test; the two kicks agree with
+    each other to the same bound."""
+    from glisser_gb300 import synth
+    m, pr, pv, r, v = synth.cartesian_state("plain-giants", 4096, seed=1000)
+    cfg = ("Time-Step 180\nTime-Block-Size 1024\nFinal-Time 1e30\nCull-Radius 0.5\nOuter-Limit 300\n"
+           "Input-File unused\nOutput-Folder unused\n")
+    sim = G.Simulation(cfg)
+    sim.set_planets(m, pr, pv)
+    sim.set_particles(r, v)
+    sim.set_kick(kick)
+    sim.init()
+    sim.loop()
+    ex = O.Exec(m, pr, pv, np.arange(len(m)), r, v, np.arange(len(r)), dt=180.0, tbsize=1024)
+    ex.loop()
+    got, want = by_id(sim.particles()), by_id(ex.particles())
+    assert np.array_equal(got["flags"], want["flags"])
+    assert sim.counts()["n_alive"] == ex.counts()["n_alive"]
+    live = want["flags"] == 0
+    err = np.linalg.norm(got["r"] - want["r"], axis=1) / np.linalg.norm(want["r"], axis=1)
+    print("kick %d: max rel pos err vs oracle %.2e" % (kick, err[live].max()))
+    assert err[live].max() < POS_TOL * 1.024
+    assert sim.stats()["borderline"] == 0
 
 
 def test_partition_stable_three_way():

@@ -63,6 +63,26 @@ def test_noalloc_partition_matches_scratch_partition_twice():
         assert c_got.cpu().numpy()[0] == (cat == 0).sum()
 
 
+def test_noalloc_partition_at_the_limit():
+    """n equal to the built-in limit fills every slot of the built-in array
+    (the last 256-particle tile included): the result is still exactly
+    glisser_partition's."""
+    n = G.partition_noalloc_max_particles()
+    rng = np.random.default_rng(11)
+    src, flags = _particles(rng, n)
+    want, got = _empty(n), _empty(n)
+    scratch = torch.zeros(G.partition_scratch_bytes(n), dtype=torch.uint8, device="cuda")
+    c_want = torch.zeros(2, dtype=torch.int32, device="cuda")
+    c_got = torch.full((2,), -1, dtype=torch.int32, device="cuda")
+    G.partition(src.view, want.view, n, scratch.data_ptr(), c_want.data_ptr(), c_want.data_ptr() + 4)
+    G.partition_noalloc(src.view, got.view, n, c_got.data_ptr(), c_got.data_ptr() + 4)
+    torch.cuda.synchronize()
+    a, b = want.host(), got.host()
+    for k in ("r", "flags", "id"):
+        assert np.array_equal(a[k], b[k]), k
+    assert np.array_equal(c_want.cpu().numpy(), c_got.cpu().numpy())
+
+
 def test_noalloc_partition_refuses_oversize():
     limit = G.partition_noalloc_max_particles()
     assert limit == 8 << 20
