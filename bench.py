@@ -476,7 +476,7 @@ def run_headline(G, args, rank, world, path, barrier, peak_tf, local):
     # the same workload: the batched kernel with the series starter, and the
     # plain kernel one system at a time (series, and the reference's classic)
     ens = make_ensemble(G, systems, T, G.STARTER_SERIES, None, (cta, ppt))
-    s_ms, s_kms, s_d, _ = time_ensemble(ens, max(2, args.steps // 2), 1, barrier)
+    s_ms, s_kms, s_d, _ = time_ensemble(ens, max(2, args.steps // 2), args.warmup, barrier)
     batched_series = s_d["particle_steps"] / (s_ms * 1e-3)
     del ens
     n_plain = args.plain_systems or len(systems)

@@ -181,12 +181,9 @@ def lib():
             "glisser_mlp_predict": ([P, F32, C.c_size_t, F32], C.c_int),
             "glisser_mlp_save": ([P, C.c_char_p], C.c_int),
             "glisser_mlp_device_weights": ([P, C.POINTER(P)], C.c_int),
-            "glisser_mlp_pack": ([F32, U32, U32], C.c_int),
             "glisser_kepler_drift_states": ([C.POINTER(ParticlesDev), C.c_size_t, C.c_double, C.c_double, C.c_int,
                                              P, P, P, P], C.c_int),
             "glisser_write_stat": ([P, C.c_char_p], C.c_int),
-            "glisser_mvs_baseline_block": ([P, P, P, P, P, C.c_size_t, C.c_uint32, C.c_uint32, P, P, P, P, P,
-                                            C.c_double, C.c_double, C.c_double, P], C.c_int),
             "glisser_swift_write_param": ([C.c_char_p, C.c_double, C.c_size_t, C.c_size_t, C.c_double, C.c_double],
                                           C.c_int),
             "glisser_swift_write_tp": ([C.c_char_p, C.c_size_t, D, D, C.c_uint32], C.c_int),

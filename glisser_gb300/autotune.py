@@ -5,7 +5,8 @@ Each candidate time-block length gets a probe ensemble (the caller's factory,
 normally every system with a subsample of its particles); on it every launch
 shape runs a warm-up block and then `blocks` timed blocks, timed on the host
 around the whole block (kernel, uploads and the overlapped host planet work),
-so the choice reflects what a run sees.  The best (T, cta, ppt) by
+so the choice reflects what a run sees.  The two warm-up blocks capture
+the launch graphs of both planet-log buffers.  The best (T, cta, ppt) by
 particle-steps per second wins.
 """
 import time
@@ -21,7 +22,8 @@ def tune_ensemble(make_probe, time_blocks=(256, 512, 1024), shapes=SHAPES, block
         ens = make_probe(T)
         for cta, ppt in shapes:
             ens.set_shape(cta, ppt)
-            ens.step()                              # warm-up (captures the graph)
+            ens.step()                              # warm-up: both buffers' graphs
+            ens.step()
             ps0 = ens.stats()["particle_steps"]
             t0 = time.perf_counter()
             for _ in range(blocks):

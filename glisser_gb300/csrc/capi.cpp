@@ -1049,13 +1049,6 @@ int glisser_mlp_save(const glisser_mlp_t* m, const char* path)
     });
 }
 
-int glisser_mlp_pack(const float* params, uint32_t* w1p, uint32_t* w2p)
-{
-    if (!params || !w1p || !w2p) return fail(nullptr, GLISSER_E_INVALID, "glisser_mlp_pack: bad arguments");
-    glisser::mlp_pack(params, w1p, w2p);
-    return GLISSER_OK;
-}
-
 int glisser_mlp_device_weights(glisser_mlp_t* m, const void** dev)
 {
     if (!m || !dev) return GLISSER_E_INVALID;

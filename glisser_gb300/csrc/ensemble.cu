@@ -394,9 +394,15 @@ void Ensemble::init()
             c[g] = r.x; c[total + g] = r.y; c[2 * total + g] = r.z;
             c[3 * total + g] = v.x; c[4 * total + g] = v.y; c[5 * total + g] = v.z;
             c[6 * total + g] = a.x; c[7 * total + g] = a.y; c[8 * total + g] = a.z;
-            // flagged at start: out of the integration with deathtime 0, its
-            // flag kept as set here (as the executor and the reference's
-            // initial partition leave it, src/executor.cu:181-187)
+            // a particle inside an encounter radius at start is removed at the
+            // end of the first block, as the reference's KillEncounterKernel
+            // does with the encounter particles its initial partition leaves in
+            // the alive range (src/executor.cu:181-187, 63-78): flagged dead
+            // here, its deathtime stamped when the first block ends
+            if (fl & 0x01) {
+                fl = (uint16_t)((fl & 0xFF00) | 0x80);
+                killed_at_start_.push_back((uint32_t)g);
+            }
             flags_[g] = fl;
             ids_[g] = (uint32_t)k;
         }
@@ -579,7 +585,6 @@ double Ensemble::step(double* gpu_ms)
         planets_device(par ^ 1);
     }
     if (nitems > 0) {
-        if (shape_.grid == 0) shape_.grid = default_grid();
         ck(cudaEventRecord(d.k0, d.stream), "event");
         if (use_graph_) {
             const BatchShape& gs = d.graph_shape[par];
@@ -645,6 +650,11 @@ double Ensemble::step(double* gpu_ms)
                     alive_[tile_sys_[t]]--;
                 }
             }
+        }
+        if (!killed_at_start_.empty()) {
+            const float tf = (float)t;
+            for (uint32_t g : killed_at_start_) deathtime_[g] = tf;
+            killed_at_start_.clear();
         }
         uint64_t after_alive = 0;
         for (auto a : alive_) after_alive += a;
@@ -740,17 +750,6 @@ void Ensemble::deaths(size_t s, std::vector<double>& deathtime, std::vector<uint
     const System& y = sys_[s];
     deathtime.assign(deathtime_.begin() + y.start, deathtime_.begin() + y.start + y.n);
     dti.assign(dti_.begin() + y.start, dti_.begin() + y.start + y.n);
-}
-
-// One wave of persistent CTAs at the occupancy the kernel reaches.
-uint32_t Ensemble::default_grid() const
-{
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    int regs_per_thread = 128;    // the tile routine's register budget
-    int per_sm = std::max(1, 65536 / (regs_per_thread * shape_.cta));
-    return (uint32_t)(sms * per_sm);
 }
 
 size_t Ensemble::alive(size_t s) const { return s < alive_.size() ? alive_[s] : 0; }

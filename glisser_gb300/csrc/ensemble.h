@@ -91,6 +91,7 @@ private:
     std::vector<uint16_t> flags_;
     std::vector<double> deathtime_;
     std::vector<uint32_t> dti_;
+    std::vector<uint32_t> killed_at_start_;   // encounter at start: deathtime stamped after the first block
     std::vector<uint32_t> ids_;
     std::vector<uint32_t> tile_first_, tile_sys_, tile_alive_;
     std::vector<uint64_t> alive_;
@@ -104,7 +105,6 @@ private:
     void rebuild_tiles(uint32_t tile);
     uint32_t write_items(int par);
     void enqueue(int par);
-    uint32_t default_grid() const;
 };
 
 }  // namespace glisser

@@ -307,6 +307,7 @@ __device__ __forceinline__ double starter_series(double T, double rinv, double a
 struct DriftResult {
     uint16_t flags;     // 0x08 unbound, 0x04 not converged
     uint16_t evals;     // Stumpff evaluations spent
+    uint16_t net;       // 1 when the drift started from the network's guess
 };
 
 // Exponent field of a float in 1..253: normal, and its reciprocal normal too.
@@ -509,49 +510,54 @@ __device__ __forceinline__ DriftInvariants drift_invariants(double rx, double ry
 // enters the energy alpha = 2 mu / r0 - v^2 of the next drift, where near
 // pericentre of an eccentric orbit any inconsistency with the vector is
 // magnified).  tol_dt = the residual tolerance times dt (KEP_TOL * dt by
-// default).  LEARNED: `guess` is the network's starting s where the kernel
-// ran the network (drifts with tau^2 >= SERIES_TAU2_MAX inside its training
-// box); a non-positive guess takes the series rule below, and the classic
-// starter is the restart when the Newton passes from the network's guess do
-// not converge.  Otherwise `starter` picks the classic or the series rule
-// (the tenth-order series while tau^2 < SERIES_TAU2_MAX, else the FP32
-// Kepler pre-solve for bound orbits and the classic starter for unbound ones).
+// default).  `starter` picks the classic or the series rule: the tenth-order
+// series while tau^2 < SERIES_TAU2_MAX, else the FP32 Kepler pre-solve for
+// bound orbits and the classic starter for unbound ones.  LEARNED (weights
+// `mlp`): where the series is outside its domain the network's guess replaces
+// the pre-solve for drifts inside its training box; it runs per lane as an
+// out-of-line call (starter_learned_call), so the lanes that take it do not
+// hold the rest of the warp to a warp-wide decision, and the classic starter
+// is the restart when the Newton passes from its guess do not converge.
 template <bool LEARNED>
 __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, double& rz, double& vx, double& vy, double& vz,
                                                    double& r2_io, double& rinv_io, const DriftInvariants& q, double dt,
-                                                   double mu, int starter, double guess, double tol_dt)
+                                                   double mu, int starter, const MlpDev* mlp, double tol_dt)
 {
     const double rinv = rinv_io;
     const double r0 = q.r0, u = q.u, mu_r = q.mu_r, alpha = q.alpha, T = q.T;
     DriftResult res;
     res.flags = __double_as_longlong(alpha) <= 0 ? 0x08 : 0;   // alpha <= 0 (or negative NaN), integer pipe
     res.evals = 0;
+    res.net = 0;
 
-    double s;
-    [[maybe_unused]] bool from_mlp = false;
-    if constexpr (LEARNED) from_mlp = guess > 0;
-    if (from_mlp) {
-        s = guess;
-    } else if (starter == STARTER_CLASSIC) {
-        s = starter_classic(dt, r0, rinv, mu, alpha, u);
-    } else {
-        if (q.tau2 < SERIES_TAU2_MAX) s = starter_series(T, rinv, alpha, u, mu_r);
-        else if (alpha > 0) s = starter_fp32_kepler(dt, r0, mu, alpha, u);
-        else s = starter_classic(dt, r0, rinv, mu, alpha, u);
+    const bool series = starter != STARTER_CLASSIC && q.tau2 < SERIES_TAU2_MAX;
+    double s = 0;
+    bool net = false;
+    if constexpr (LEARNED) {
+        if (starter != STARTER_CLASSIC && !series) {
+            s = starter_learned_call(mlp, T, rinv, q.tau2, u, mu_r, alpha);
+            net = s > 0;     // -1 outside the training box (NaN fails too)
+        }
     }
-
+    // One Newton call site: the starter's s, then, after a network guess
+    // that did not converge, the classic restart.
     const double tol = tol_dt;
     GFun g;
     double ds = 0;
-    bool ok = kepler_newton(s, dt, r0, u, mu, alpha, tol, g, ds, res.evals);
-    if constexpr (LEARNED) {
-        if (!ok && from_mlp) {
-            s = starter_classic(dt, r0, rinv, mu, alpha, u);
-            ok = kepler_newton(s, dt, r0, u, mu, alpha, tol, g, ds, res.evals);
+    bool ok = false, restart = false;
+    for (;;) {
+        if (!net || restart) {
+            if (series && !restart) s = starter_series(T, rinv, alpha, u, mu_r);
+            else if (starter != STARTER_CLASSIC && !restart && alpha > 0) s = starter_fp32_kepler(dt, r0, mu, alpha, u);
+            else s = starter_classic(dt, r0, rinv, mu, alpha, u);
         }
+        ok = kepler_newton(s, dt, r0, u, mu, alpha, tol, g, ds, res.evals);
+        if (ok || !net || restart) break;
+        restart = true;
     }
     if (!ok) ok = kepler_laguerre(s, dt, r0, u, mu, alpha, tol, g, ds, res.evals);
     if (!ok) res.flags |= 0x04;
+    res.net = net;
     // g: the G-functions at the root (the last evaluation's when not converged)
     const double g3 = g.g3, g2 = g.g2, g1 = g.g1;
 
@@ -570,20 +576,14 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
     return res;
 }
 
-// The same drift for a single particle: invariants and, LEARNED, the scalar
-// network (weights `mlp`) evaluated here where the kernels run it (tau^2 at
-// or above SERIES_TAU2_MAX).
+// The same drift for a single particle, its invariants formed here.
 template <bool LEARNED>
 __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, double& rz, double& vx, double& vy, double& vz,
                                                    double& r2_io, double& rinv_io, double dt, double mu, int starter,
                                                    const MlpDev* mlp, double tol_dt)
 {
     const DriftInvariants q = drift_invariants(rx, ry, rz, vx, vy, vz, r2_io, rinv_io, dt, mu);
-    double guess = -1.0;
-    if constexpr (LEARNED) {
-        if (!(q.tau2 < SERIES_TAU2_MAX)) guess = starter_learned(mlp, q.T, rinv_io, q.tau2, q.u, q.mu_r, q.alpha);
-    }
-    return kepler_drift<LEARNED>(rx, ry, rz, vx, vy, vz, r2_io, rinv_io, q, dt, mu, starter, guess, tol_dt);
+    return kepler_drift<LEARNED>(rx, ry, rz, vx, vy, vz, r2_io, rinv_io, q, dt, mu, starter, mlp, tol_dt);
 }
 
 }  // namespace glisser

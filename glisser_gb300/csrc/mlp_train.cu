@@ -5,11 +5,9 @@
 // Training kernel layout: one CTA of 128 threads takes a tile of 128
 // samples, one per thread.  Each thread runs the forward pass of its sample
 // in the order of mlp_forward, the inputs and the hidden activations rounded
-// to the BF16 hi + lo pairs the tensor-core layers read (gradients straight
-// through the rounding), so the trained network is the one the drift
-// evaluates; it
-// keeps the pre-activations of the second layer in
-// registers, and runs the backward pass to the per-sample deltas, which it
+// to the BF16 hi + lo pairs its products read (gradients straight through
+// the rounding), so the trained network is the one the drift evaluates; it
+// keeps the pre-activations of the second layer in registers, and runs the backward pass to the per-sample deltas, which it
 // writes to shared-memory tiles (rows padded to 33 floats: the row-per-thread
 // writes and the column reads are both bank-conflict free).  The weight
 // gradients are then sums over the tile's samples -- the FP32-accumulated
@@ -288,29 +286,24 @@ __global__ void adam_kernel(float* params, float* m, float* v, const float* __re
     params[p] -= a.lr * (mm / a.bc1) / (sqrtf(vv / a.bc2) + a.eps);
 }
 
-// The time-block kernels' inference (the warp's tensor cores,
-// mlp_forward_warp) over a feature list (NaN outside the box).  Every lane
-// runs the network, lanes past n on zero inputs.
+// The time-block kernels' inference (mlp_forward) over a feature list (NaN
+// outside the box).
 __global__ void __launch_bounds__(128) predict_kernel(const MlpDev* __restrict__ w, const float* __restrict__ feat,
                                                       uint32_t n, float* y)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
     const MlpNorm& nm = w->norm;
-    float x0 = 0.0f, x1 = 0.0f, x2 = 0.0f;
-    bool in_box = false;
-    if (i < n) {
-        const float f0 = feat[3 * (size_t)i], f1 = feat[3 * (size_t)i + 1], f2 = feat[3 * (size_t)i + 2];
-        in_box = f0 >= nm.x_lo[0] && f0 <= nm.x_hi[0] && f1 >= nm.x_lo[1] && f1 <= nm.x_hi[1] && f2 >= nm.x_lo[2] &&
-                 f2 <= nm.x_hi[2];
-        if (in_box) {
-            x0 = (f0 - nm.in_mean[0]) * nm.in_scale[0];
-            x1 = (f1 - nm.in_mean[1]) * nm.in_scale[1];
-            x2 = (f2 - nm.in_mean[2]) * nm.in_scale[2];
-        }
+    const float f0 = feat[3 * (size_t)i], f1 = feat[3 * (size_t)i + 1], f2 = feat[3 * (size_t)i + 2];
+    const bool in_box = f0 >= nm.x_lo[0] && f0 <= nm.x_hi[0] && f1 >= nm.x_lo[1] && f1 <= nm.x_hi[1] &&
+                        f2 >= nm.x_lo[2] && f2 <= nm.x_hi[2];
+    if (!in_box) {
+        y[i] = __int_as_float(0x7fc00000);
+        return;
     }
-    __syncwarp();
-    const float out = mlp_forward_warp(w, x0, x1, x2);
-    if (i < n) y[i] = in_box ? fmaf(nm.out_scale, out, nm.out_mean) : __int_as_float(0x7fc00000);
+    const float out = mlp_forward(w, (f0 - nm.in_mean[0]) * nm.in_scale[0], (f1 - nm.in_mean[1]) * nm.in_scale[1],
+                                  (f2 - nm.in_mean[2]) * nm.in_scale[2]);
+    y[i] = fmaf(nm.out_scale, out, nm.out_mean);
 }
 
 // One Kepler drift per state with the time-block kernel's drift routine.
@@ -359,21 +352,8 @@ MlpDev make_dev(const float* params, const MlpNorm& norm)
     std::memset(&d, 0, sizeof d);
     for (int j = 0; j < MLP_H; j++) {
         for (int k = 0; k < MLP_IN; k++) d.w1[j][k] = bf16_round_host(params[MLP_OFF_W1 + j * MLP_IN + k]);
-        {
-            // the layer-1 MMA's B pairs: W1's columns at k = 0-2 and again at 3-5
-            const uint32_t b0 = bf16_bits_round(params[MLP_OFF_W1 + j * MLP_IN]) >> 16;
-            const uint32_t b1 = bf16_bits_round(params[MLP_OFF_W1 + j * MLP_IN + 1]) >> 16;
-            const uint32_t b2 = bf16_bits_round(params[MLP_OFF_W1 + j * MLP_IN + 2]) >> 16;
-            d.w1p[j][0] = b0 | (b1 << 16);
-            d.w1p[j][1] = b2 | (b0 << 16);
-            d.w1p[j][2] = b1 | (b2 << 16);
-            d.w1p[j][3] = 0u;
-        }
         d.b1[j] = params[MLP_OFF_B1 + j];
         for (int k = 0; k < MLP_H; k++) d.w2[j][k] = bf16_round_host(params[MLP_OFF_W2 + j * MLP_H + k]);
-        for (int q = 0; q < MLP_H / 2; q++)
-            d.w2p[j][q] = (bf16_bits_round(params[MLP_OFF_W2 + j * MLP_H + 2 * q]) >> 16) |
-                          (bf16_bits_round(params[MLP_OFF_W2 + j * MLP_H + 2 * q + 1]) & 0xFFFF0000u);
         d.b2[j] = params[MLP_OFF_B2 + j];
         d.w3[j] = bf16_round_host(params[MLP_OFF_W3 + j]);
     }
@@ -383,15 +363,6 @@ MlpDev make_dev(const float* params, const MlpNorm& norm)
 }
 
 }  // namespace
-
-void mlp_pack(const float* params, uint32_t* w1p, uint32_t* w2p)
-{
-    MlpNorm norm;
-    std::memset(&norm, 0, sizeof norm);
-    const MlpDev d = make_dev(params, norm);
-    std::memcpy(w1p, d.w1p, sizeof d.w1p);
-    std::memcpy(w2p, d.w2p, sizeof d.w2p);
-}
 
 void* mlp_upload(const std::vector<uint8_t>& file)
 {

@@ -29,11 +29,6 @@ struct MlpFileHeader {
 int drift_states(const glisser_particles* pa, size_t n, double dt, double mu, int starter, const void* mlp,
                  uint32_t* evals, uint16_t* flags, cudaStream_t stream);
 
-// The tensor-core operands the inference routine reads, as the device copy
-// holds them: W1 as the layer-1 MMA's B pairs [32][4] and W2 as the hidden
-// layer's B pairs [32][16] (BF16 pairs, low half first).
-void mlp_pack(const float* params, uint32_t* w1p, uint32_t* w2p);
-
 // Device copy of a weights file (validated), and its release.
 void* mlp_upload(const std::vector<uint8_t>& file);
 void mlp_free(void* dev);

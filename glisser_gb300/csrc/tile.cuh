@@ -265,46 +265,14 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
             const double* Ld = Lw + (size_t)s * rec;
 #pragma unroll
             for (int k = 0; k < PPT; k++) {
-                DriftInvariants q;
-                double guess = -1.0;
-                if constexpr (LEARNED) {
-                    // The network runs where the series starter is outside its
-                    // domain (tau^2 >= SERIES_TAU2_MAX: a step that is a sizeable
-                    // part of the local dynamical time), in place of the FP32
-                    // pre-solve; elsewhere the series starter does.  It runs on
-                    // the warp's tensor cores, so the decision is warp-uniform:
-                    // all lanes evaluate it (zero inputs for a lane that does not
-                    // need it).  Every lane of the warp reaches this point on
-                    // every step and every k -- no lane may leave the step or
-                    // particle loops early while LEARNED is set, or the MMAs
-                    // below would run with part of the warp.
-                    bool want = false;
-                    if (flags[k] == 0) {
-                        q = drift_invariants(rx[k], ry[k], rz[k], vx[k], vy[k], vz[k], r2[k], rinv[k], p.dt, mu);
-                        want = !(q.tau2 < SERIES_TAU2_MAX);
-                    }
-                    if (__any_sync(0xffffffffu, want)) {
-                        float x0 = 0.0f, x1 = 0.0f, x2 = 0.0f;
-                        const bool in_box = want && mlp_inputs(p.mlp, q.tau2, q.u, rinv[k], q.mu_r, q.alpha, x0, x1, x2);
-                        if (!in_box) x0 = x1 = x2 = 0.0f;
-#ifdef GLISSER_MLP_INLINE
-                        const float y = mlp_forward_warp(p.mlp, x0, x1, x2);
-#else
-                        const float y = mlp_forward_warp_call(p.mlp, x0, x1, x2);
-#endif
-                        if (in_box) {
-                            guess = learned_guess(p.mlp, q.T, q.tau2, y);
-                            nets++;
-                        }
-                    }
-                }
                 if (flags[k] != 0) continue;
-                if constexpr (!LEARNED)
-                    q = drift_invariants(rx[k], ry[k], rz[k], vx[k], vy[k], vz[k], r2[k], rinv[k], p.dt, mu);
+                const DriftInvariants q =
+                    drift_invariants(rx[k], ry[k], rz[k], vx[k], vy[k], vz[k], r2[k], rinv[k], p.dt, mu);
                 DriftResult d = kepler_drift<LEARNED>(rx[k], ry[k], rz[k], vx[k], vy[k], vz[k], r2[k], rinv[k], q,
-                                                       p.dt, mu, p.starter, guess, p.tol_dt);
+                                                       p.dt, mu, p.starter, p.mlp, p.tol_dt);
                 uint16_t fl = d.flags;
                 evals += d.evals;
+                if constexpr (LEARNED) nets += d.net;
                 double aax, aay, aaz;
                 if constexpr (KICK64) {
                     aax = Ld[0]; aay = Ld[1]; aaz = Ld[2];
@@ -364,9 +332,7 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
     for (int k = 0; k < PPT; k++) {
         const uint32_t off = (uint32_t)k * CTA + tid;
         const uint32_t i = first + off;
-        // a particle flagged before the block (the ensemble kernel's tiles keep
-        // removed particles in place) was not integrated: nothing to store
-        const bool active = off < count && flags0[k] == 0;
+        const bool active = off < count;
         if (active) {
             if (p.kill == GLISSER_ENCOUNTERS_KILL && (flags[k] & 0x01))
                 flags[k] = (uint16_t)((flags[k] & 0xFF00) | 0x80);

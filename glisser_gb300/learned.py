@@ -155,17 +155,6 @@ class Trainer:
         return d.value
 
 
-def pack(params):
-    """The inference routine's tensor-core B operands for the flattened
-    parameters: (w1p [32, 4], w2p [32, 16]) uint32 BF16 pairs."""
-    from . import U32
-    p = np.ascontiguousarray(params, np.float32)
-    w1p = np.zeros((32, 4), np.uint32)
-    w2p = np.zeros((32, 16), np.uint32)
-    _check(lib().glisser_mlp_pack(_p(p, F32), _p(w1p, U32), _p(w2p, U32)))
-    return w1p, w2p
-
-
 def drift_states(r, v, dt, mu, starter=STARTER_SERIES, trainer=None):
     """One Kepler drift of each state on cuda:0 through the time-block
     kernel's drift routine; returns (r, v, evals, flags) on the host."""

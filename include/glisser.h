@@ -491,27 +491,9 @@ int glisser_mlp_gradients(glisser_mlp_t *m, const float *feat, const float *targ
 int glisser_mlp_predict(glisser_mlp_t *m, const float *feat, size_t n, float *y);
 /* Weights file for glisser_set_starter / glisser_ensemble_set_starter. */
 int glisser_mlp_save(const glisser_mlp_t *m, const char *path);
-/* The tensor-core operands of the drift's inference for the flattened
- * parameters (host memory, no device needed): W1 as the layer-1 MMA's B
- * operand w1p [32][4] and W2 as the hidden layer's w2p [32][16], BF16 pairs
- * with the lower index in the low half.  For checking the packing. */
-int glisser_mlp_pack(const float *params, uint32_t *w1p, uint32_t *w2p);
 /* The current weights as the drift reads them (device pointer owned by m,
  * valid until the next change of weights or normalisation). */
 int glisser_mlp_device_weights(glisser_mlp_t *m, const void **dev);
-
-/* Measurement only: the reference's particle time block as the reference
- * runs it on a GPU -- its arithmetic (src/wh.cu:43-177: elliptic drift with
- * five fixed Newton passes, a sin/cos pair each) and its layout (24-byte
- * 3-vectors for r, v, a; planet logs read from global memory; one particle
- * per thread, the thrust::for_each launch of src/wh.cu:344-395) -- for timing
- * glisser_integrate_timeblock against it on the same GPU.  Device arrays:
- * r, v, a [n][3]; h0_log [tbsize][3]; r_log [tbsize][planet_n - 1][3]; m,
- * id, rh [planet_n]; mu = m[0].  Asynchronous on `stream`. */
-int glisser_mvs_baseline_block(double *r, double *v, double *a, uint16_t *flags, uint32_t *deathtime_index,
-                               size_t n, uint32_t tbsize, uint32_t planet_n, const double *h0_log,
-                               const double *r_log, const double *m, const uint32_t *id, const double *rh,
-                               double outer_radius, double dt, double mu, void *stream);
 
 /* One Kepler drift by dt of each device state [0, n) (r, v updated in place)
  * with the time-block kernel's drift routine and the given starter (`mlp`:

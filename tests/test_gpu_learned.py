@@ -140,10 +140,10 @@ def test_inference_matches_oracle(trained):
     y_ref = M.predict(tr.params, tr.norm, feat.astype(np.float64))
     ok = np.isfinite(y_ref)
     assert np.array_equal(np.isfinite(y_gpu), ok)
-    # the GPU runs the time-block kernels' inference: both layers on the
-    # tensor cores, the inputs and the hidden activations each read as a BF16
-    # hi + lo pair.  The FP32 values and the oracle's float64 ones can round
-    # to different pairs at a rounding boundary (2^-17 of the value), for the
+    # the GPU runs the time-block kernels' inference (mlp_forward: FP32 FMAs,
+    # the inputs and the hidden activations each read as a BF16 hi + lo
+    # pair).  The FP32 values and the oracle's float64 ones can round to
+    # different pairs at a rounding boundary (2^-17 of the value), for the
     # inputs and for the activations alike, hence the looser bound on the few
     # largest differences.
     scale = float(tr.norm["out_scale"])

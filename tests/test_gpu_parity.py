@@ -148,40 +148,3 @@ def test_partition_stable_three_way():
     assert np.array_equal(out["r"], r[order])
     c = counts.cpu().numpy()
     assert c[0] == (cat == 0).sum() and c[1] == (cat == 1).sum()
-
-
-@pytest.mark.parametrize("case", ["neptune_t128", "giants_t256", "flags_t64", "hill_t64"])
-def test_reference_layout_kernel_matches_oracle(case):
-    """glisser_mvs_baseline_block (the measurement kernel that runs the
-    reference's arithmetic in the reference's GPU layout) against the oracle's
-    restatement of MVSKernel on the fixture's first block: flags and
-    deathtime indices exact, states to rounding (the device contracts
-    multiply-adds and uses its own sin/cos)."""
-    d, cfg = load(case)
-    dt = float(cfg["Time-Step"])
-    outer = float(cfg.get("Outer-Limit", 300))
-    r, v, a = d["r0"].copy(), d["v0"].copy(), d["a0"].copy()
-    fl0 = d["flags0"].astype(np.uint16)
-    T = len(d["blk0_h0_log"])
-    npl = len(d["blk0_m"])
-    ro, vo, ao = r.copy(), v.copy(), a.copy()
-    fo, dto = O.block(ro, vo, ao, fl0, T, npl, d["blk0_h0_log"], d["blk0_r_log"], d["blk0_m"], d["blk0_id"],
-                      d["blk0_rh"], outer, dt, float(d["blk0_m"][0]), drift="mvs")
-    dev = torch.device("cuda:0")
-    t = {k: torch.tensor(x, dtype=torch.float64, device=dev).contiguous() for k, x in (("r", r), ("v", v), ("a", a))}
-    tf = torch.tensor(fl0.view(np.int16), device=dev)
-    td = torch.zeros(len(r), dtype=torch.int32, device=dev)
-    pl = {k: torch.tensor(np.ascontiguousarray(d["blk0_" + k]), dtype=torch.float64, device=dev)
-          for k in ("h0_log", "r_log", "m", "rh")}
-    pid = torch.tensor(d["blk0_id"].astype(np.uint32).view(np.int32), device=dev)
-    rc = G.lib().glisser_mvs_baseline_block(t["r"].data_ptr(), t["v"].data_ptr(), t["a"].data_ptr(), tf.data_ptr(),
-                                            td.data_ptr(), len(r), T, npl, pl["h0_log"].data_ptr(),
-                                            pl["r_log"].data_ptr(), pl["m"].data_ptr(), pid.data_ptr(),
-                                            pl["rh"].data_ptr(), outer, dt, float(d["blk0_m"][0]), None)
-    assert rc == 0
-    torch.cuda.synchronize()
-    assert np.array_equal(tf.cpu().numpy().view(np.uint16), fo)
-    assert np.array_equal(td.cpu().numpy().view(np.uint32), dto)
-    from gpu_util import rel_err
-    assert rel_err(t["r"].cpu().numpy(), ro).max() < 1e-11
-    assert rel_err(t["v"].cpu().numpy(), vo).max() < 1e-11
