@@ -509,7 +509,8 @@ def run_headline(G, args, rank, world, path, barrier, peak_tf, local):
         "particles": n_total, "time_block": T, "shape": {"threads_per_cta": cta, "particles_per_thread": ppt},
         "autotune": [{"T": a, "cta": b, "ppt": c, "rate": r} for a, b, c, r in tune["table"]],
         "gpu_launches": d["launches"], "evals_per_particle_step": d["kepler_evals"] / max(d["particle_steps"], 1),
-        "network_drifts": d["learned_drifts"], "borderline_tests": d["borderline"],
+        "network_drifts": d["learned_drifts"], "wide_drifts": d["wide_drifts"],
+        "network_blocks": d["network_blocks"], "borderline_tests": d["borderline"],
         "clocks": clk, "e2e": e2e, "roofline": roofline,
         "batched_series": batched_series, "plain_series_one_at_a_time": plain_series,
         "plain_classic_one_at_a_time": plain_classic, "plain_systems_sampled": n_plain,
@@ -558,7 +559,9 @@ def timed_blocks(G, sim, blocks):
     return {"value": ps / el, "unit": UNIT, "kernel_ms_per_block": kms / blocks,
             "kernel_rate": ps / (kms * 1e-3), "kepler_evals_per_particle_step":
                 (s1["kepler_evals"] - s0["kepler_evals"]) / max(ps, 1),
-            "network_drifts": s1["learned_drifts"] - s0["learned_drifts"], "particle_steps": ps,
+            "network_drifts": s1["learned_drifts"] - s0["learned_drifts"],
+            "wide_drifts": s1["wide_drifts"] - s0["wide_drifts"],
+            "network_blocks": s1["network_blocks"] - s0["network_blocks"], "particle_steps": ps,
             "borderline_tests": s1["borderline"] - s0["borderline"], "launches": s1["launches"] - s0["launches"]}
 
 
@@ -937,7 +940,9 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": ENSEMBLE_WORKLOAD + "; learned starter, batched persistent kernel, CUDA graphs",
                        "systems": 256, "particles_per_gpu": head["particles"], "time_block": head["time_block"],
-                       "n_planets": 4, "starter": "learned (series where it applies, network elsewhere)",
+                       "n_planets": 4,
+                       "starter": "learned (series where it applies, network elsewhere; per-block dispatch: the "
+                                  "network kernel after a block with drifts at tau^2 >= 0.01)",
                        "shape": head["shape"], "parallelism": "independent ensembles per GPU",
                        "l2": "inputs larger than L2 (%.0f MB of particle state)" % (head["particles"] * 90 / 1e6)},
             "vs_plain": value / head["plain_series_one_at_a_time"],
@@ -953,7 +958,8 @@ def main():
             "roofline": head["roofline"],
             "kernel_ms_per_block": head["kernel_ms_per_block"],
             "kepler_evals_per_particle_step": head["evals_per_particle_step"],
-            "network_drifts": head["network_drifts"], "borderline_tests": head["borderline_tests"],
+            "network_drifts": head["network_drifts"], "wide_drifts": head["wide_drifts"],
+            "network_blocks": head["network_blocks"], "borderline_tests": head["borderline_tests"],
             "gpu_launches": head["gpu_launches"],
             "clocks": head["clocks"],
             "e2e": head["e2e"],

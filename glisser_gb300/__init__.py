@@ -74,7 +74,8 @@ class MlpNorm(C.Structure):
 class HandoffDev(C.Structure):
     _fields_ = [("count", C.c_void_p), ("index", C.c_void_p), ("id", C.c_void_p), ("flags", C.c_void_p),
                 ("deathtime_index", C.c_void_p), ("capacity", C.c_uint32), ("reserved", C.c_uint32),
-                ("status", C.c_void_p), ("evals", C.c_void_p), ("borderline", C.c_void_p), ("learned", C.c_void_p)]
+                ("status", C.c_void_p), ("evals", C.c_void_p), ("borderline", C.c_void_p), ("learned", C.c_void_p),
+                ("wide", C.c_void_p)]
 
 
 _lib = None
@@ -116,6 +117,10 @@ def lib():
             "glisser_ensemble_borderline": ([P, C.POINTER(C.c_ulonglong)], C.c_int),
             "glisser_learned_drifts": ([P, C.POINTER(C.c_ulonglong)], C.c_int),
             "glisser_ensemble_learned_drifts": ([P, C.POINTER(C.c_ulonglong)], C.c_int),
+            "glisser_wide_drifts": ([P, C.POINTER(C.c_ulonglong)], C.c_int),
+            "glisser_ensemble_wide_drifts": ([P, C.POINTER(C.c_ulonglong)], C.c_int),
+            "glisser_network_blocks": ([P, C.POINTER(C.c_ulonglong)], C.c_int),
+            "glisser_ensemble_network_blocks": ([P, C.POINTER(C.c_ulonglong)], C.c_int),
             "glisser_step_block": ([P, C.POINTER(C.c_int), D, D], C.c_int),
             "glisser_run": ([P, C.c_int], C.c_int),
             "glisser_finish": ([P], C.c_int),
@@ -404,10 +409,12 @@ class Simulation:
         lib().glisser_stats(self.h, C.byref(ps), C.byref(ev))
         lib().glisser_launches(self.h, C.byref(ln))
         lib().glisser_borderline(self.h, C.byref(bl))
-        ld = C.c_ulonglong()
+        ld, wd, nb = C.c_ulonglong(), C.c_ulonglong(), C.c_ulonglong()
         lib().glisser_learned_drifts(self.h, C.byref(ld))
+        lib().glisser_wide_drifts(self.h, C.byref(wd))
+        lib().glisser_network_blocks(self.h, C.byref(nb))
         return dict(particle_steps=ps.value, kepler_evals=ev.value, launches=ln.value, borderline=bl.value,
-                    learned_drifts=ld.value)
+                    learned_drifts=ld.value, wide_drifts=wd.value, network_blocks=nb.value)
 
     def stream(self):
         s = C.c_void_p()
@@ -632,10 +639,12 @@ class Ensemble:
         ps, ev, ln, bl = C.c_ulonglong(), C.c_ulonglong(), C.c_ulonglong(), C.c_ulonglong()
         lib().glisser_ensemble_stats(self.h, C.byref(ps), C.byref(ev), C.byref(ln))
         lib().glisser_ensemble_borderline(self.h, C.byref(bl))
-        ld = C.c_ulonglong()
+        ld, wd, nb = C.c_ulonglong(), C.c_ulonglong(), C.c_ulonglong()
         lib().glisser_ensemble_learned_drifts(self.h, C.byref(ld))
+        lib().glisser_ensemble_wide_drifts(self.h, C.byref(wd))
+        lib().glisser_ensemble_network_blocks(self.h, C.byref(nb))
         return dict(particle_steps=ps.value, kepler_evals=ev.value, launches=ln.value, borderline=bl.value,
-                    learned_drifts=ld.value)
+                    learned_drifts=ld.value, wide_drifts=wd.value, network_blocks=nb.value)
 
     @property
     def t(self):

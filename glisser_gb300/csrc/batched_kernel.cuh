@@ -21,9 +21,9 @@ using namespace tile;
 
 // Persistent kernel over (system, tile) work items.  Register budget: 128
 // per thread (512 resident threads per SM).  The learned starter runs its
-// network only in a warp-uniform branch where the series starter is outside
-// its domain and is held to the same budget (what the network needs beyond
-// it is spilled around that branch).
+// network per lane, as an out-of-line call, only where the series starter is
+// outside its domain, and is held to the same budget (what the network needs
+// beyond it is saved around that call).
 template <int NP, int CTA, int PPT, bool LEARNED, bool KICK64>
 __global__ void __launch_bounds__(CTA, (LEARNED ? GLISSER_BATCHED_THREADS_PER_SM_LEARNED
                                                 : GLISSER_BATCHED_THREADS_PER_SM) / CTA)

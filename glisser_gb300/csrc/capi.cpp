@@ -581,6 +581,20 @@ int glisser_learned_drifts(const glisser_t* h, unsigned long long* drifts)
     return GLISSER_OK;
 }
 
+int glisser_wide_drifts(const glisser_t* h, unsigned long long* drifts)
+{
+    if (!h || !drifts) return GLISSER_E_INVALID;
+    *drifts = h->ex->wide_drifts();
+    return GLISSER_OK;
+}
+
+int glisser_network_blocks(const glisser_t* h, unsigned long long* blocks)
+{
+    if (!h || !blocks) return GLISSER_E_INVALID;
+    *blocks = h->ex->network_blocks();
+    return GLISSER_OK;
+}
+
 int glisser_launches(const glisser_t* h, unsigned long long* launches)
 {
     if (!h || !launches) return GLISSER_E_INVALID;
@@ -844,6 +858,20 @@ int glisser_ensemble_learned_drifts(const glisser_ensemble_t* e, unsigned long l
 {
     if (!e || !drifts) return GLISSER_E_INVALID;
     *drifts = e->e->learned_drifts();
+    return GLISSER_OK;
+}
+
+int glisser_ensemble_wide_drifts(const glisser_ensemble_t* e, unsigned long long* drifts)
+{
+    if (!e || !drifts) return GLISSER_E_INVALID;
+    *drifts = e->e->wide_drifts();
+    return GLISSER_OK;
+}
+
+int glisser_ensemble_network_blocks(const glisser_ensemble_t* e, unsigned long long* blocks)
+{
+    if (!e || !blocks) return GLISSER_E_INVALID;
+    *blocks = e->e->network_blocks();
     return GLISSER_OK;
 }
 

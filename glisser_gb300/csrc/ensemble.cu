@@ -91,12 +91,14 @@ struct Ensemble::Dev {
     uint16_t* d_ho_flags = nullptr;
     uint32_t *h_ho_index = nullptr, *h_ho_dti = nullptr;
     uint16_t* h_ho_flags = nullptr;
-    cudaGraphExec_t graph[2] = {};
-    BatchShape graph_shape[2] = {};
-    uint32_t graph_len[2] = {};
-    int graph_starter[2] = { -1, -1 };
-    double graph_tol[2] = { -1, -1 };
-    int graph_kick[2] = { -1, -1 };
+    // one graph per staging parity and starter kernel (slot = parity + 2 x
+    // network kernel)
+    cudaGraphExec_t graph[4] = {};
+    BatchShape graph_shape[4] = {};
+    uint32_t graph_len[4] = {};
+    int graph_starter[4] = { -1, -1, -1, -1 };
+    double graph_tol[4] = { -1, -1, -1, -1 };
+    int graph_kick[4] = { -1, -1, -1, -1 };
     void* d_mlp = nullptr;            // learned-starter weights
     // device planet integrator state ([S][npl] arrays, one allocation)
     PlanetSysDev pl{};
@@ -105,7 +107,7 @@ struct Ensemble::Dev {
     uint32_t* h_status = nullptr;
     cudaStream_t pstream = nullptr;
     cudaEvent_t planets_done = nullptr;
-    int mlp_version = 0, graph_mlp[2] = { 0, 0 };
+    int mlp_version = 0, graph_mlp[4] = { 0, 0, 0, 0 };
     double* h_state = nullptr;        // pinned staging of whole-ensemble state transfers
     uint16_t* h_state_flags = nullptr;
 
@@ -118,8 +120,9 @@ struct Ensemble::Dev {
         cudaFreeHost(h_status);
         if (planets_done) cudaEventDestroy(planets_done);
         if (pstream) cudaStreamDestroy(pstream);
+        for (int g = 0; g < 4; g++)
+            if (graph[g]) cudaGraphExecDestroy(graph[g]);
         for (int b = 0; b < 2; b++) {
-            if (graph[b]) cudaGraphExecDestroy(graph[b]);
             cudaFree(d_log[b]); cudaFree(d_m[b]); cudaFree(d_rh[b]); cudaFree(d_id[b]);
             cudaFree(d_items[b]); cudaFree(d_nitems[b]);
             cudaFreeHost(h_log[b]); cudaFreeHost(h_m[b]); cudaFreeHost(h_rh[b]); cudaFreeHost(h_id[b]);
@@ -191,6 +194,7 @@ void Ensemble::set_starter(int s, const std::vector<uint8_t>* mlp_file)
         dev_->mlp_version++;
     }
     starter_ = s;
+    net_next_ = true;
 }
 
 void Ensemble::set_system(size_t s, size_t npl, const double* m, const double* r, const double* v, size_t n,
@@ -455,9 +459,9 @@ void Ensemble::init()
         d.h_nitems[b] = hmalloc<uint32_t>(1, "pinned");
     }
     d.d_ctr = dmalloc<uint32_t>(8, "cudaMalloc counters");
-    d.d_evals = dmalloc<unsigned long long>(3, "cudaMalloc evals");
+    d.d_evals = dmalloc<unsigned long long>(4, "cudaMalloc evals");
     d.h_ctr = hmalloc<uint32_t>(8, "pinned");
-    d.h_evals = hmalloc<unsigned long long>(3, "pinned");
+    d.h_evals = hmalloc<unsigned long long>(4, "pinned");
     d.d_ho_index = dmalloc<uint32_t>(cap, "cudaMalloc hand-off");
     d.d_ho_id = dmalloc<uint32_t>(cap, "cudaMalloc hand-off");
     d.d_ho_dti = dmalloc<uint32_t>(cap, "cudaMalloc hand-off");
@@ -521,8 +525,11 @@ void Ensemble::init()
     }
 }
 
-// Enqueues one block on the stream: uploads, counter reset, kernel, counters back.
-void Ensemble::enqueue(int par)
+// Enqueues one block on the stream: uploads, counter reset, kernel, counters
+// back.  `starter` is the block's kernel: the learned one, or the series
+// one in its place on a block after one without drifts outside the series
+// starter's domain.
+void Ensemble::enqueue(int par, int starter)
 {
     Dev& d = *dev_;
     const size_t S = sys_.size();
@@ -540,14 +547,14 @@ void Ensemble::enqueue(int par)
                        d.stream), "items");
     ck(cudaMemcpyAsync(d.d_nitems[par], d.h_nitems[par], sizeof(uint32_t), cudaMemcpyHostToDevice, d.stream), "n");
     ck(cudaMemsetAsync(d.d_ctr, 0, 8 * sizeof(uint32_t), d.stream), "memset");
-    ck(cudaMemsetAsync(d.d_evals, 0, 3 * sizeof(unsigned long long), d.stream), "memset");
+    ck(cudaMemsetAsync(d.d_evals, 0, 4 * sizeof(unsigned long long), d.stream), "memset");
     BatchSystems sy{ d.d_log[par], log_stride_, d.d_m[par], d.d_rh[par], d.d_id[par] };
     glisser_step_params sp{};
     sp.dt = cfg.dt;
     sp.outer_radius = cfg.outer_radius;
-    sp.starter = starter_;
+    sp.starter = starter;
     sp.kill_encounters = 1;
-    sp.mlp = starter_ == GLISSER_STARTER_LEARNED ? d.d_mlp : nullptr;
+    sp.mlp = starter == GLISSER_STARTER_LEARNED ? d.d_mlp : nullptr;
     sp.kepler_tol = kepler_tol_;
     sp.kick = kick_;
     glisser_handoff ho{};
@@ -561,11 +568,12 @@ void Ensemble::enqueue(int par)
     ho.evals = d.d_evals;
     ho.borderline = d.d_evals + 1;
     ho.learned = d.d_evals + 2;
+    ho.wide = d.d_evals + 3;
     int rc = launch_batched(&d.pa, sy, d.d_items[par], d.d_nitems[par], d.d_ctr + 2, npl_, len_, &sp, &ho, shape_,
                             d.stream);
     if (rc != GLISSER_OK) throw CudaError(std::string("batched launch failed: ") + timeblock_error());
     ck(cudaMemcpyAsync(d.h_ctr, d.d_ctr, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, d.stream), "counters");
-    ck(cudaMemcpyAsync(d.h_evals, d.d_evals, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, d.stream),
+    ck(cudaMemcpyAsync(d.h_evals, d.d_evals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, d.stream),
        "evals");
 }
 
@@ -585,33 +593,37 @@ double Ensemble::step(double* gpu_ms)
         planets_device(par ^ 1);
     }
     if (nitems > 0) {
+        const bool net = starter_ == GLISSER_STARTER_LEARNED && net_next_;
+        const int starter = starter_ == GLISSER_STARTER_LEARNED && !net ? GLISSER_STARTER_SERIES : starter_;
+        net_blocks_ += net;
         ck(cudaEventRecord(d.k0, d.stream), "event");
         if (use_graph_) {
-            const BatchShape& gs = d.graph_shape[par];
-            bool stale = !d.graph[par] || gs.cta != shape_.cta || gs.ppt != shape_.ppt || gs.grid != shape_.grid ||
-                         d.graph_len[par] != len_ || d.graph_starter[par] != starter_ ||
-                         d.graph_mlp[par] != d.mlp_version || d.graph_tol[par] != kepler_tol_ ||
-                         d.graph_kick[par] != kick_;
+            const int slot = par + (net ? 2 : 0);
+            const BatchShape& gs = d.graph_shape[slot];
+            bool stale = !d.graph[slot] || gs.cta != shape_.cta || gs.ppt != shape_.ppt || gs.grid != shape_.grid ||
+                         d.graph_len[slot] != len_ || d.graph_starter[slot] != starter ||
+                         d.graph_mlp[slot] != d.mlp_version || d.graph_tol[slot] != kepler_tol_ ||
+                         d.graph_kick[slot] != kick_;
             if (stale) {
-                if (d.graph[par]) cudaGraphExecDestroy(d.graph[par]);
-                d.graph[par] = nullptr;
+                if (d.graph[slot]) cudaGraphExecDestroy(d.graph[slot]);
+                d.graph[slot] = nullptr;
                 cudaGraph_t g;
                 ck(cudaStreamBeginCapture(d.stream, cudaStreamCaptureModeRelaxed), "begin capture");
-                enqueue(par);
+                enqueue(par, starter);
                 ck(cudaStreamEndCapture(d.stream, &g), "end capture");
-                ck(cudaGraphInstantiate(&d.graph[par], g, 0), "instantiate");
+                ck(cudaGraphInstantiate(&d.graph[slot], g, 0), "instantiate");
                 cudaGraphDestroy(g);
-                d.graph_len[par] = len_;
-                d.graph_shape[par] = shape_;
-                d.graph_starter[par] = starter_;
-                d.graph_mlp[par] = d.mlp_version;
-                d.graph_tol[par] = kepler_tol_;
-                d.graph_kick[par] = kick_;
+                d.graph_len[slot] = len_;
+                d.graph_shape[slot] = shape_;
+                d.graph_starter[slot] = starter;
+                d.graph_mlp[slot] = d.mlp_version;
+                d.graph_tol[slot] = kepler_tol_;
+                d.graph_kick[slot] = kick_;
             }
-            ck(cudaGraphLaunch(d.graph[par], d.stream), "graph launch");
+            ck(cudaGraphLaunch(d.graph[slot], d.stream), "graph launch");
             launches_ += 1;
         } else {
-            enqueue(par);
+            enqueue(par, starter);
             launches_ += 1;
         }
         ck(cudaEventRecord(d.k1, d.stream), "event");
@@ -630,6 +642,8 @@ double Ensemble::step(double* gpu_ms)
         evals_ += d.h_evals[0];
         borderline_ += d.h_evals[1];
         learned_ += d.h_evals[2];
+        wide_ += d.h_evals[3];
+        net_next_ = d.h_evals[3] > 0;
         uint64_t dti_sum = 0;
         if (k) {
             ck(cudaMemcpy(d.h_ho_index, d.d_ho_index, k * sizeof(uint32_t), cudaMemcpyDeviceToHost), "hand-off");
@@ -707,12 +721,22 @@ void Ensemble::put_state(size_t n, const double* r, const double* v)
     ensure_state_staging();
     Dev& d = *dev_;
     double* st = d.h_state;
+    // a state at tau^2 = dt^2 mu / r^3 >= 0.01 about the heaviest central
+    // mass brings the learned starter's network kernel back for the next block
+    double mu = 0;
+    for (const System& y : sys_) mu = std::max(mu, y.pl.m.empty() ? 0.0 : y.pl.m[0]);
+    const double rw = std::cbrt(100.0 * cfg.dt * cfg.dt * mu), rw2 = rw * rw;
+    std::atomic<bool> near{ false };
     parallel_for(n, [&](size_t b, size_t e) {
+        bool nr = false;
         for (size_t k = b; k < e; k++) {
             st[k] = r[3 * k]; st[n + k] = r[3 * k + 1]; st[2 * n + k] = r[3 * k + 2];
             st[3 * n + k] = v[3 * k]; st[4 * n + k] = v[3 * k + 1]; st[5 * n + k] = v[3 * k + 2];
+            nr |= r[3 * k] * r[3 * k] + r[3 * k + 1] * r[3 * k + 1] + r[3 * k + 2] * r[3 * k + 2] <= rw2;
         }
+        if (nr) near.store(true, std::memory_order_relaxed);
     });
+    if (near.load()) net_next_ = true;
     double* dst[6] = { d.pa.rx, d.pa.ry, d.pa.rz, d.pa.vx, d.pa.vy, d.pa.vz };
     for (int k = 0; k < 6; k++)
         ck(cudaMemcpyAsync(dst[k], st + k * n, n * sizeof(double), cudaMemcpyHostToDevice, d.stream), "upload state");

@@ -65,6 +65,8 @@ public:
     unsigned long long kepler_evals() const { return evals_; }
     unsigned long long borderline_tests() const { return borderline_; }
     unsigned long long learned_drifts() const { return learned_; }
+    unsigned long long wide_drifts() const { return wide_; }
+    unsigned long long network_blocks() const { return net_blocks_; }
     unsigned long long launches() const { return launches_; }
 
 private:
@@ -95,7 +97,10 @@ private:
     std::vector<uint32_t> ids_;
     std::vector<uint32_t> tile_first_, tile_sys_, tile_alive_;
     std::vector<uint64_t> alive_;
-    unsigned long long psteps_ = 0, evals_ = 0, launches_ = 0, borderline_ = 0, learned_ = 0;
+    unsigned long long psteps_ = 0, evals_ = 0, launches_ = 0, borderline_ = 0, learned_ = 0, wide_ = 0;
+    // the learned starter's per-block dispatch (as the executor's)
+    bool net_next_ = true;
+    unsigned long long net_blocks_ = 0;
 
     void planet_block(size_t s, int par);
     void ensure_state_staging();
@@ -104,7 +109,7 @@ private:
     void check_planet_status();
     void rebuild_tiles(uint32_t tile);
     uint32_t write_items(int par);
-    void enqueue(int par);
+    void enqueue(int par, int starter);
 };
 
 }  // namespace glisser

@@ -304,6 +304,7 @@ void Executor::set_starter(int starter, const std::vector<uint8_t>* blob)
         d_->d_mlp = mlp_upload(*blob);
     }
     starter_ = starter;
+    net_next_ = true;
 }
 
 // helio_acc_particle<old=true> at the first step (src/wh.cpp:611-657): the
@@ -664,9 +665,9 @@ void Executor::init()
     }
     size_t cap = std::max<size_t>(n, 1);
     ck(cudaMalloc(&d.d_ctr, 16 * sizeof(uint32_t)), "cudaMalloc counters");
-    ck(cudaMalloc(&d.d_evals, 3 * sizeof(unsigned long long)), "cudaMalloc evals");
+    ck(cudaMalloc(&d.d_evals, 4 * sizeof(unsigned long long)), "cudaMalloc evals");
     ck(cudaMallocHost(&d.h_ctr, 16 * sizeof(uint32_t)), "pinned");
-    ck(cudaMallocHost(&d.h_evals, 3 * sizeof(unsigned long long)), "pinned");
+    ck(cudaMallocHost(&d.h_evals, 4 * sizeof(unsigned long long)), "pinned");
     ck(cudaMalloc(&d.d_ho_index, cap * sizeof(uint32_t)), "cudaMalloc hand-off");
     ck(cudaMalloc(&d.d_ho_id, cap * sizeof(uint32_t)), "cudaMalloc hand-off");
     ck(cudaMalloc(&d.d_ho_dti, cap * sizeof(uint32_t)), "cudaMalloc hand-off");
@@ -720,7 +721,7 @@ bool Executor::step_block(double* cpu_ms, double* gpu_ms)
         launches_total_ += 3;   // count, scan, scatter
         if (rc != GLISSER_OK) throw CudaError("partition launch failed");
         ck(cudaMemcpyAsync(d.h_ctr, d.d_ctr, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, d.main), "counters");
-        ck(cudaMemcpyAsync(d.h_evals, d.d_evals, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, d.main),
+        ck(cudaMemcpyAsync(d.h_evals, d.d_evals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, d.main),
            "evals");
         ck(cudaEventRecord(d.done, d.main), "event");
         d.cur = nxt;
@@ -729,7 +730,7 @@ bool Executor::step_block(double* cpu_ms, double* gpu_ms)
     };
     if (n_range > 0) {
         ck(cudaMemsetAsync(d.d_ctr, 0, 16 * sizeof(uint32_t), d.main), "memset counters");
-        ck(cudaMemsetAsync(d.d_evals, 0, 3 * sizeof(unsigned long long), d.main), "memset evals");
+        ck(cudaMemsetAsync(d.d_evals, 0, 4 * sizeof(unsigned long long), d.main), "memset evals");
     }
     if (n_kernel > 0) {
         ck(cudaStreamWaitEvent(d.main, d.uploaded[used], 0), "wait upload");
@@ -744,9 +745,11 @@ bool Executor::step_block(double* cpu_ms, double* gpu_ms)
         glisser_step_params sp{};
         sp.dt = cur_dt_;
         sp.outer_radius = cfg.outer_radius;
-        sp.starter = starter_;
+        const bool net = starter_ == GLISSER_STARTER_LEARNED && net_next_;
+        sp.starter = starter_ == GLISSER_STARTER_LEARNED && !net ? GLISSER_STARTER_SERIES : starter_;
         sp.kill_encounters = cfg.resolve_encounters ? GLISSER_ENCOUNTERS_ROLLBACK : GLISSER_ENCOUNTERS_KILL;
-        sp.mlp = starter_ == GLISSER_STARTER_LEARNED ? d.d_mlp : nullptr;
+        sp.mlp = net ? d.d_mlp : nullptr;
+        net_blocks_ += net;
         sp.kepler_tol = kepler_tol_;
         sp.kick = kick_;
         glisser_handoff ho{};
@@ -760,6 +763,7 @@ bool Executor::step_block(double* cpu_ms, double* gpu_ms)
         ho.evals = d.d_evals;
         ho.borderline = d.d_evals + 1;
         ho.learned = d.d_evals + 2;
+        ho.wide = d.d_evals + 3;
         ck(cudaEventRecord(d.start, d.main), "event");
         int rc = launch_timeblock(&d.buf[d.cur].p, n_kernel, &pb, &sp, &ho, d.main);
         if (rc != GLISSER_OK) throw CudaError(std::string("time-block launch failed: ") + timeblock_error());
@@ -795,6 +799,8 @@ bool Executor::step_block(double* cpu_ms, double* gpu_ms)
         evals_total_ += d.h_evals[0];
         borderline_total_ += d.h_evals[1];
         learned_total_ += d.h_evals[2];
+        wide_total_ += d.h_evals[3];
+        if (n_kernel > 0) net_next_ = d.h_evals[3] > 0;
         // both particle buffers must agree on the particles that left the
         // partitioned range this block (the next partition reads only one)
         if (n0 + n1 < n_range) {

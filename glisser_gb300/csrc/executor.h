@@ -87,6 +87,8 @@ public:
     unsigned long long borderline_tests() const { return borderline_total_; }
     // drifts started from the learned starter's network guess since init
     unsigned long long learned_drifts() const { return learned_total_; }
+    unsigned long long wide_drifts() const { return wide_total_; }
+    unsigned long long network_blocks() const { return net_blocks_; }
     unsigned long long particle_steps() const { return psteps_total_; }
     unsigned long long launches() const { return launches_total_; }
     void* stream() const;
@@ -124,7 +126,12 @@ private:
     int kick_ = GLISSER_KICK_FLOAT_FLOAT;
     bool device_output_ = true;
     uint32_t max_id_ = 0;
-    unsigned long long evals_total_ = 0, borderline_total_ = 0, learned_total_ = 0;
+    unsigned long long evals_total_ = 0, borderline_total_ = 0, learned_total_ = 0, wide_total_ = 0;
+    // the learned starter's per-block dispatch: the network kernel runs when
+    // the previous block had a drift outside the series starter's domain
+    // (and on the first block)
+    bool net_next_ = true;
+    unsigned long long net_blocks_ = 0;
     unsigned long long psteps_total_ = 0;
     unsigned long long launches_total_ = 0;
 

@@ -308,6 +308,7 @@ struct DriftResult {
     uint16_t flags;     // 0x08 unbound, 0x04 not converged
     uint16_t evals;     // Stumpff evaluations spent
     uint16_t net;       // 1 when the drift started from the network's guess
+    uint16_t wide;      // 1 when tau^2 >= SERIES_TAU2_MAX (series and learned starters)
 };
 
 // Exponent field of a float in 1..253: normal, and its reciprocal normal too.
@@ -514,10 +515,12 @@ __device__ __forceinline__ DriftInvariants drift_invariants(double rx, double ry
 // series while tau^2 < SERIES_TAU2_MAX, else the FP32 Kepler pre-solve for
 // bound orbits and the classic starter for unbound ones.  LEARNED (weights
 // `mlp`): where the series is outside its domain the network's guess replaces
-// the pre-solve for drifts inside its training box; it runs per lane as an
-// out-of-line call (starter_learned_call), so the lanes that take it do not
-// hold the rest of the warp to a warp-wide decision, and the classic starter
-// is the restart when the Newton passes from its guess do not converge.
+// the pre-solve for drifts inside its training box; it runs per lane, inline
+// with a small register footprint (mlp_forward), so the lanes that take it
+// do not hold the rest of the warp to a warp-wide decision and the drift
+// keeps its registers.  When the Newton passes
+// from its guess do not converge, the classic starter is the restart, for
+// the bounded Laguerre iteration that is every starter's last resort.
 template <bool LEARNED>
 __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, double& rz, double& vx, double& vy, double& vz,
                                                    double& r2_io, double& rinv_io, const DriftInvariants& q, double dt,
@@ -531,29 +534,25 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
     res.net = 0;
 
     const bool series = starter != STARTER_CLASSIC && q.tau2 < SERIES_TAU2_MAX;
-    double s = 0;
-    bool net = false;
+    res.wide = starter != STARTER_CLASSIC && !series;
+    double s = -1.0;
     if constexpr (LEARNED) {
-        if (starter != STARTER_CLASSIC && !series) {
-            s = starter_learned_call(mlp, T, rinv, q.tau2, u, mu_r, alpha);
-            net = s > 0;     // -1 outside the training box (NaN fails too)
-        }
+        if (res.wide) s = starter_learned(mlp, T, rinv, q.tau2, u, mu_r, alpha);
     }
-    // One Newton call site: the starter's s, then, after a network guess
-    // that did not converge, the classic restart.
+    const bool net = s > 0;     // -1 outside the training box (NaN fails too)
+    if (!net) {
+        if (series) s = starter_series(T, rinv, alpha, u, mu_r);
+        else if (res.wide && alpha > 0) s = starter_fp32_kepler(dt, r0, mu, alpha, u);
+        else s = starter_classic(dt, r0, rinv, mu, alpha, u);
+    }
     const double tol = tol_dt;
     GFun g;
     double ds = 0;
-    bool ok = false, restart = false;
-    for (;;) {
-        if (!net || restart) {
-            if (series && !restart) s = starter_series(T, rinv, alpha, u, mu_r);
-            else if (starter != STARTER_CLASSIC && !restart && alpha > 0) s = starter_fp32_kepler(dt, r0, mu, alpha, u);
-            else s = starter_classic(dt, r0, rinv, mu, alpha, u);
-        }
-        ok = kepler_newton(s, dt, r0, u, mu, alpha, tol, g, ds, res.evals);
-        if (ok || !net || restart) break;
-        restart = true;
+    bool ok = kepler_newton(s, dt, r0, u, mu, alpha, tol, g, ds, res.evals);
+    if constexpr (LEARNED) {
+        // a network guess whose Newton passes did not converge: the
+        // classic starter, then the bounded Laguerre iteration from it
+        if (!ok && net) s = starter_classic(dt, r0, rinv, mu, alpha, u);
     }
     if (!ok) ok = kepler_laguerre(s, dt, r0, u, mu, alpha, tol, g, ds, res.evals);
     if (!ok) res.flags |= 0x04;

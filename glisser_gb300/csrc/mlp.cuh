@@ -19,11 +19,10 @@
 // inputs (the normalised features, the hidden activations) as the sum of
 // two BF16 values (hi = the value rounded, lo = the remainder rounded: ~16
 // significant bits) and accumulate in FP32 FMAs.  The time-block kernels run
-// it per particle (mlp_forward, as the out-of-line starter_learned_call) only
-// in drifts where the series starter is outside its domain, so the lanes of
-// a warp that need it run it alone; the training kernels compute the same
-// forward pass in the same order, so the network is trained on the
-// arithmetic it is used with.
+// it per particle (mlp_forward) only in drifts where the series starter is
+// outside its domain, so the lanes of a warp that need it run it alone; the
+// training kernels compute the same forward pass in the same order, so the
+// network is trained on the arithmetic it is used with.
 #pragma once
 #include <cuda_bf16.h>
 #include <cstdint>
@@ -76,15 +75,20 @@ __device__ __forceinline__ float bf16_split_sum(float h)
 __device__ __forceinline__ float mlp_sigmoid(float a) { return __fdividef(1.0f, 1.0f + __expf(-a)); }
 
 // Network output (normalised units) for normalised inputs x0..x2, per
-// thread in FP32.  Weight rows are read with 16-byte loads; every thread of
-// a warp reads the same address, so each load is one broadcast transaction.
+// thread in FP32.  It runs inline in the time-block kernels' drift, whose
+// hot path holds most of the register file, so its footprint is kept small:
+// the loops are not unrolled, the hidden activations live in thread-local
+// memory (touched only when the network runs) and one weight row at a time
+// is in registers -- no register of the drift's state is given up for it.
+// Weight rows are read with 16-byte loads; every thread of a warp reads the
+// same address, so each load is one broadcast transaction.
 __device__ __forceinline__ float mlp_forward(const MlpDev* __restrict__ w, float x0, float x1, float x2)
 {
     x0 = bf16_split_sum(x0);
     x1 = bf16_split_sum(x1);
     x2 = bf16_split_sum(x2);
     float h1[MLP_H];
-#pragma unroll
+#pragma unroll 1
     for (int j = 0; j < MLP_H; j++) {
         const float4 r = __ldg(reinterpret_cast<const float4*>(w->w1[j]));
         float a = __ldg(&w->b1[j]);
@@ -94,11 +98,11 @@ __device__ __forceinline__ float mlp_forward(const MlpDev* __restrict__ w, float
         h1[j] = bf16_split_sum(a * mlp_sigmoid(a));
     }
     float y = __ldg(&w->b3);
-#pragma unroll 2
+#pragma unroll 1
     for (int j = 0; j < MLP_H; j++) {
         float a = __ldg(&w->b2[j]);
         const float4* row = reinterpret_cast<const float4*>(w->w2[j]);
-#pragma unroll
+#pragma unroll 1
         for (int q = 0; q < MLP_H / 4; q++) {
             const float4 r = __ldg(row + q);
             a = fmaf(r.x, h1[4 * q], a);
@@ -155,17 +159,6 @@ __device__ __forceinline__ double starter_learned(const MlpDev* __restrict__ w, 
     float x0, x1, x2;
     if (!mlp_inputs(w, tau2, u, rinv, mu_r, alpha, x0, x1, x2)) return -1.0;
     return learned_guess(w, T, tau2, mlp_forward(w, x0, x1, x2));
-}
-
-// starter_learned as an out-of-line call, for kernels that run the network
-// only in a rarely taken branch: the call boundary keeps the network's 32
-// hidden activations out of the register allocation of the kernel's main
-// path (the caller's live values are saved and restored around the call,
-// only when it is taken).
-static __device__ __noinline__ double starter_learned_call(const MlpDev* __restrict__ w, double T, double rinv,
-                                                           float tau2, double u, double mu_r, double alpha)
-{
-    return starter_learned(w, T, rinv, tau2, u, mu_r, alpha);
 }
 
 }  // namespace glisser

@@ -199,7 +199,7 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
     double rx[PPT], ry[PPT], rz[PPT], vx[PPT], vy[PPT], vz[PPT], ax[PPT], ay[PPT], az[PPT], r2[PPT], rinv[PPT];
     uint16_t flags[PPT], flags0[PPT];
     uint32_t dti[PPT];
-    uint32_t evals = 0, border = 0, nets = 0;
+    uint32_t evals = 0, border = 0, nets = 0, wide = 0;
     const double hdt = p.dt * 0.5;
     const double mu = sh.m[0];
     const double rh2_sun = sh.rh2[0];
@@ -273,6 +273,7 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
                 uint16_t fl = d.flags;
                 evals += d.evals;
                 if constexpr (LEARNED) nets += d.net;
+                wide += d.wide;
                 double aax, aay, aaz;
                 if constexpr (KICK64) {
                     aax = Ld[0]; aay = Ld[1]; aaz = Ld[2];
@@ -378,6 +379,12 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
         if (lane == 0 && e) atomicAdd(p.ho.borderline, e);
+    }
+    if (p.ho.wide) {
+        unsigned long long e = wide;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
+        if (lane == 0 && e) atomicAdd(p.ho.wide, e);
     }
     if constexpr (LEARNED) {
         if (p.ho.learned) {

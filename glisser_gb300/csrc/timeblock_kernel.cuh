@@ -18,10 +18,10 @@ using namespace tile;
 #define GLISSER_TB_MIN_BLOCKS 10
 #endif
 
-// The learned-starter kernel runs the network only in a warp-uniform branch
-// taken where the series starter is outside its domain; it is held to the
-// plain kernel's occupancy, so that the registers the network needs on top
-// of the drift's are spilled around that branch instead of lowering the
+// The learned-starter kernel runs the network per lane, as an out-of-line
+// call, only where the series starter is outside its domain; it is held to
+// the plain kernel's occupancy, so that the registers the network needs on
+// top of the drift's are saved around that call instead of lowering the
 // occupancy of every step.
 #ifndef GLISSER_TB_MIN_BLOCKS_LEARNED
 #define GLISSER_TB_MIN_BLOCKS_LEARNED GLISSER_TB_MIN_BLOCKS

@@ -128,7 +128,10 @@ typedef struct glisser_step_params {
  * squared distance lay within about 2^-40 (9e-13) of the squared radius, where
  * two correct evaluations that round differently could flag differently.
  * `learned` (optional) accumulates the drifts started from the learned
- * starter's network guess. */
+ * starter's network guess.  `wide` (optional) accumulates the drifts outside
+ * the series starter's domain (tau^2 = (dt / r0)^2 mu / r0 >= 0.01) under the
+ * series and learned starters: the drifts where the learned starter's
+ * network may run. */
 typedef struct glisser_handoff {
     uint32_t *count;
     uint32_t *index;             /* position in the particle arrays */
@@ -141,6 +144,7 @@ typedef struct glisser_handoff {
     unsigned long long *evals;
     unsigned long long *borderline;
     unsigned long long *learned;
+    unsigned long long *wide;
 } glisser_handoff;
 
 #define GLISSER_STATUS_LOG_TIMEOUT 0x1u   /* planet-log staging wait gave up */
@@ -319,7 +323,14 @@ int glisser_swift_write_stat(const glisser_swift_stats *s, const char *path);
 /* Selects the Kepler starter (default GLISSER_STARTER_SERIES) and, for the
  * learned starter, the weights blob written by glisser_mlp_save.  The learned
  * starter takes the series starter where it applies (tau^2 = dt^2 mu / r0^3
- * below 0.01) and the network's guess elsewhere inside its training box. */
+ * below 0.01) and the network's guess elsewhere inside its training box.
+ * Dispatch per block: the first block after init, and every block after one
+ * in which some drift had tau^2 >= 0.01 (glisser_wide_drifts), launches the
+ * kernel with the network; a block after one without such a drift launches
+ * the kernel without it -- the same arithmetic for every drift below 0.01,
+ * without the network's code and registers, which cost a few per cent even
+ * where it does not run.  A drift that reaches 0.01 in such a block takes the
+ * series rule's FP32 pre-solve, and the next block runs the network again. */
 int glisser_set_starter(glisser_t *h, int starter, const char *mlp_path);
 
 /* Running totals since init: particle-steps integrated (each particle counts
@@ -334,6 +345,13 @@ int glisser_borderline(const glisser_t *h, unsigned long long *tests);
 /* Drifts started from the learned starter's network guess since init (the
  * rest of a learned run took the series rule).  No reference counterpart. */
 int glisser_learned_drifts(const glisser_t *h, unsigned long long *drifts);
+/* Drifts outside the series starter's domain since init (tau^2 >= 0.01;
+ * glisser_handoff.wide), under the series and learned starters.  No
+ * reference counterpart. */
+int glisser_wide_drifts(const glisser_t *h, unsigned long long *drifts);
+/* Blocks launched with the learned starter's network kernel since init (the
+ * per-block dispatch of glisser_set_starter). */
+int glisser_network_blocks(const glisser_t *h, unsigned long long *blocks);
 /* Kernel launches issued by the executor since init, and its CUDA stream
  * (a cudaStream_t; the blocks' kernels and copies run on it). */
 int glisser_launches(const glisser_t *h, unsigned long long *launches);
@@ -370,6 +388,10 @@ int glisser_ensemble_set_kick(glisser_ensemble_t *e, int kick);
 int glisser_ensemble_borderline(const glisser_ensemble_t *e, unsigned long long *tests);
 /* Drifts started from the network guess since init (as glisser_learned_drifts). */
 int glisser_ensemble_learned_drifts(const glisser_ensemble_t *e, unsigned long long *drifts);
+/* Drifts outside the series starter's domain since init (as glisser_wide_drifts). */
+int glisser_ensemble_wide_drifts(const glisser_ensemble_t *e, unsigned long long *drifts);
+/* Blocks launched with the network kernel since init (as glisser_network_blocks). */
+int glisser_ensemble_network_blocks(const glisser_ensemble_t *e, unsigned long long *blocks);
 /* Planets of system s at the particles' time: m[npl], r/v[npl][3]
  * (heliocentric); *n receives npl, cap is the room in m / r / v. */
 int glisser_ensemble_get_planets(glisser_ensemble_t *e, size_t s, double *m, double *r, double *v, size_t cap,

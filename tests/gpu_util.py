@@ -50,7 +50,7 @@ class DevHandoff:
     def __init__(self, capacity):
         dev = torch.device("cuda:0")
         self.ctr = torch.zeros(4, dtype=torch.int32, device=dev)
-        self.evals = torch.zeros(3, dtype=torch.int64, device=dev)
+        self.evals = torch.zeros(4, dtype=torch.int64, device=dev)
         self.index = torch.zeros(max(capacity, 1), dtype=torch.int32, device=dev)
         self.ids = torch.zeros(max(capacity, 1), dtype=torch.int32, device=dev)
         self.flags = torch.zeros(max(capacity, 1), dtype=torch.int16, device=dev)
@@ -58,7 +58,7 @@ class DevHandoff:
         self.view = G.HandoffDev(self.ctr.data_ptr(), self.index.data_ptr(), self.ids.data_ptr(),
                                  self.flags.data_ptr(), self.dti.data_ptr(), capacity, 0,
                                  self.ctr.data_ptr() + 4, self.evals.data_ptr(), self.evals.data_ptr() + 8,
-                                 self.evals.data_ptr() + 16)
+                                 self.evals.data_ptr() + 16, self.evals.data_ptr() + 24)
 
     def reset(self):
         self.ctr.zero_()
@@ -70,6 +70,7 @@ class DevHandoff:
         k = int(c[0])
         ev = self.evals.cpu().numpy()
         return dict(count=k, status=int(c[1]), evals=int(ev[0]), borderline=int(ev[1]), learned=int(ev[2]),
+                    wide=int(ev[3]),
                     index=self.index[:k].cpu().numpy().view(np.uint32), id=self.ids[:k].cpu().numpy().view(np.uint32),
                     flags=self.flags[:k].cpu().numpy().view(np.uint16), dti=self.dti[:k].cpu().numpy().view(np.uint32))
 

@@ -202,6 +202,10 @@ def test_simulation_learned_matches_series(trained, workload, T, blocks):
     err = np.linalg.norm(a[0]["r"] - b[0]["r"], axis=1) / np.linalg.norm(a[0]["r"], axis=1)
     assert err[live].max() < 1e-10, err[live].max()
     assert a[2]["particle_steps"] == b[2]["particle_steps"]
+    # both workloads have drifts with tau^2 >= 0.01 in every block, where the
+    # learned run's network kernel runs
+    assert b[2]["network_blocks"] == blocks and a[2]["network_blocks"] == 0
+    assert 0 < b[2]["learned_drifts"] <= b[2]["wide_drifts"]
 
 
 def test_ensemble_learned_matches_series_and_is_launch_invariant(trained):
