@@ -60,8 +60,6 @@ ENSEMBLE_WORKLOAD = ("ensembles: 256 systems (Sun + 4 giants, masses x U(0.9,1.1
 # kernels whose rooflines the bench reports; the captures and their commands
 # are summarised under profiles/.
 FP64_COUNTS = {
-    "batched_kernel<4,64,1,learned>": {"dadd": 2.0, "dfma": 31.1, "dmul": 21.1, "pipe_busy": 0.72,
-                                       "profile": "profiles/batched_kernel_ensembles.md"},
     "timeblock_kernel<4>": {"dadd": 2.0, "dfma": 31.1, "dmul": 21.1, "pipe_busy": 0.719,
                             "profile": "profiles/timeblock_kernel_plain-giants.md"},
 }
@@ -83,6 +81,10 @@ def executed_fp64(kernel, rate, peak_tf):
     peak.  A DADD or DMUL fills an FP64 issue slot with one flop, so `frac`
     counts flops and `fp64_pipe_busy` the slots."""
     c = FP64_COUNTS.get(kernel)
+    if c is None:
+        # per-thread instruction counts do not depend on the CTA size
+        c = next((v for k, v in FP64_COUNTS.items() if k.split("<")[0] == kernel.split("<")[0] and
+                  k.split(",")[0] == kernel.split(",")[0] and k.split(",")[2:] == kernel.split(",")[2:]), None)
     if c is None or not rate:
         return None
     flops = c["dadd"] + c["dmul"] + 2 * c["dfma"]
@@ -483,8 +485,11 @@ def run_headline(G, args, rank, world, path, barrier, peak_tf, local):
     plain_series = plain_one_at_a_time(G, systems, T, G.STARTER_SERIES, n_plain)
     plain_classic = plain_one_at_a_time(G, systems, T, G.STARTER_CLASSIC, n_plain)
 
-    kernel = "batched_kernel<4,%d,%d,learned>" % (cta, ppt)
-    ex = executed_fp64("batched_kernel<4,64,1,learned>" if (cta, ppt) == (64, 1) else kernel, kernel_rate, peak_tf)
+    # the kernel the timed blocks ran: under the learned starter's per-block
+    # dispatch the network kernel only after blocks with drifts at tau^2 >= 0.01
+    variant = "learned" if d["network_blocks"] else "series"
+    kernel = "batched_kernel<4,%d,%d,%s>" % (cta, ppt, variant)
+    ex = executed_fp64(kernel, kernel_rate, peak_tf)
     F = alg_flops_per_particle_step(4)
     traffic = DRAM_BYTES_PER_PARTICLE_BLOCK * n_total
     roofline = {

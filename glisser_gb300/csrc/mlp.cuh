@@ -77,40 +77,60 @@ __device__ __forceinline__ float mlp_sigmoid(float a) { return __fdividef(1.0f, 
 // Network output (normalised units) for normalised inputs x0..x2, per
 // thread in FP32.  It runs inline in the time-block kernels' drift, whose
 // hot path holds most of the register file, so its footprint is kept small:
-// the loops are not unrolled, the hidden activations live in thread-local
-// memory (touched only when the network runs) and one weight row at a time
-// is in registers -- no register of the drift's state is given up for it.
+// the outer loops are not unrolled, the hidden activations live in
+// thread-local memory (touched only when the network runs) and a few weight
+// rows at a time are in registers -- no register of the drift's state is
+// given up for it.
 // Weight rows are read with 16-byte loads; every thread of a warp reads the
 // same address, so each load is one broadcast transaction.
+// Rows of the hidden layer computed together: each activation read from
+// thread-local memory serves MLP_ROWS rows, and the rows' FMA chains are
+// independent, so the network's latency (it holds up the warp it runs in)
+// is a fraction of a row-at-a-time loop's.  Each row's sum keeps the order
+// of the training kernels' forward pass.
+constexpr int MLP_ROWS = 4;
+
 __device__ __forceinline__ float mlp_forward(const MlpDev* __restrict__ w, float x0, float x1, float x2)
 {
     x0 = bf16_split_sum(x0);
     x1 = bf16_split_sum(x1);
     x2 = bf16_split_sum(x2);
-    float h1[MLP_H];
+    float4 h1[MLP_H / 4];
 #pragma unroll 1
-    for (int j = 0; j < MLP_H; j++) {
-        const float4 r = __ldg(reinterpret_cast<const float4*>(w->w1[j]));
-        float a = __ldg(&w->b1[j]);
-        a = fmaf(r.x, x0, a);
-        a = fmaf(r.y, x1, a);
-        a = fmaf(r.z, x2, a);
-        h1[j] = bf16_split_sum(a * mlp_sigmoid(a));
+    for (int q = 0; q < MLP_H / 4; q++) {
+        float h[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            const int j = 4 * q + c;
+            const float4 r = __ldg(reinterpret_cast<const float4*>(w->w1[j]));
+            float a = __ldg(&w->b1[j]);
+            a = fmaf(r.x, x0, a);
+            a = fmaf(r.y, x1, a);
+            a = fmaf(r.z, x2, a);
+            h[c] = bf16_split_sum(a * mlp_sigmoid(a));
+        }
+        h1[q] = make_float4(h[0], h[1], h[2], h[3]);
     }
     float y = __ldg(&w->b3);
 #pragma unroll 1
-    for (int j = 0; j < MLP_H; j++) {
-        float a = __ldg(&w->b2[j]);
-        const float4* row = reinterpret_cast<const float4*>(w->w2[j]);
+    for (int j = 0; j < MLP_H; j += MLP_ROWS) {
+        float a[MLP_ROWS];
+#pragma unroll
+        for (int k = 0; k < MLP_ROWS; k++) a[k] = __ldg(&w->b2[j + k]);
 #pragma unroll 1
         for (int q = 0; q < MLP_H / 4; q++) {
-            const float4 r = __ldg(row + q);
-            a = fmaf(r.x, h1[4 * q], a);
-            a = fmaf(r.y, h1[4 * q + 1], a);
-            a = fmaf(r.z, h1[4 * q + 2], a);
-            a = fmaf(r.w, h1[4 * q + 3], a);
+            const float4 h = h1[q];
+#pragma unroll
+            for (int k = 0; k < MLP_ROWS; k++) {
+                const float4 r = __ldg(reinterpret_cast<const float4*>(w->w2[j + k]) + q);
+                a[k] = fmaf(r.x, h.x, a[k]);
+                a[k] = fmaf(r.y, h.y, a[k]);
+                a[k] = fmaf(r.z, h.z, a[k]);
+                a[k] = fmaf(r.w, h.w, a[k]);
+            }
         }
-        y = fmaf(__ldg(&w->w3[j]), a * mlp_sigmoid(a), y);
+#pragma unroll
+        for (int k = 0; k < MLP_ROWS; k++) y = fmaf(__ldg(&w->w3[j + k]), a[k] * mlp_sigmoid(a[k]), y);
     }
     return y;
 }
