@@ -60,12 +60,15 @@ ENSEMBLE_WORKLOAD = ("ensembles: 256 systems (Sun + 4 giants, masses x U(0.9,1.1
 # kernels whose rooflines the bench reports; the captures and their commands
 # are summarised under profiles/.
 FP64_COUNTS = {
+    "batched_kernel<4,128,1,series>": {"dadd": 2.0, "dfma": 33.0, "dmul": 22.0, "pipe_busy": 0.796,
+                                       "profile": "profiles/batched_kernel_ensembles.md"},
     "timeblock_kernel<4>": {"dadd": 2.0, "dfma": 31.1, "dmul": 21.1, "pipe_busy": 0.719,
                             "profile": "profiles/timeblock_kernel_plain-giants.md"},
 }
 # DRAM bytes per particle per block of the batched kernel (ncu dram__bytes_read
-# + dram__bytes_write on a capture of the headline workload's kernel)
-DRAM_BYTES_PER_PARTICLE_BLOCK = 160.0
+# + dram__bytes_write, 150.8 + 66.6 MB, on a capture of one block of a quarter
+# of the headline workload: 1,537,972 particles, T = 1024)
+DRAM_BYTES_PER_PARTICLE_BLOCK = 141.4
 
 
 def alg_flops_per_particle_step(n_planets, k_ref=5):
@@ -80,16 +83,18 @@ def executed_fp64(kernel, rate, peak_tf):
     particle-step, ncu counts) at `rate` particle-steps/s, against the probe
     peak.  A DADD or DMUL fills an FP64 issue slot with one flop, so `frac`
     counts flops and `fp64_pipe_busy` the slots."""
-    c = FP64_COUNTS.get(kernel)
-    if c is None:
+    key = kernel if kernel in FP64_COUNTS else None
+    if key is None:
         # per-thread instruction counts do not depend on the CTA size
-        c = next((v for k, v in FP64_COUNTS.items() if k.split("<")[0] == kernel.split("<")[0] and
-                  k.split(",")[0] == kernel.split(",")[0] and k.split(",")[2:] == kernel.split(",")[2:]), None)
+        key = next((k for k in FP64_COUNTS if k.split(",")[0] == kernel.split(",")[0] and
+                    k.split(",")[2:] == kernel.split(",")[2:]), None)
+    c = FP64_COUNTS.get(key)
     if c is None or not rate:
         return None
     flops = c["dadd"] + c["dmul"] + 2 * c["dfma"]
     tf = rate * flops / 1e12
-    return {"kernel": kernel, "instructions_per_particle_step": round(c["dadd"] + c["dmul"] + c["dfma"], 1),
+    return {"kernel": kernel, "counts_from": key,
+            "instructions_per_particle_step": round(c["dadd"] + c["dmul"] + c["dfma"], 1),
             "flops_per_particle_step": flops, "achieved": tf, "peak": peak_tf, "unit": "TFLOP/s",
             "frac": tf / peak_tf if peak_tf else None, "fp64_pipe_busy": c["pipe_busy"], "source": c["profile"]}
 

@@ -407,7 +407,10 @@ int glisser_ensemble_get_particles(glisser_ensemble_t *e, size_t s, double *r, d
  * velocities the next block integrates (accelerations, flags and death
  * records stay), get_state reads them (and the flags) back; it waits for the
  * blocks in flight.  With r, v and flags all NULL get_state only reports *n.
- * For a host that keeps the state in its own buffers between blocks. */
+ * For a host that keeps the state in its own buffers between blocks.  Under
+ * the learned starter a new state with a particle at tau^2 >= 0.01 about the
+ * ensemble's heaviest central mass runs the next block with the network
+ * kernel. */
 int glisser_ensemble_set_state(glisser_ensemble_t *e, size_t n, const double *r, const double *v);
 int glisser_ensemble_get_state(glisser_ensemble_t *e, double *r, double *v, uint16_t *flags, size_t cap, size_t *n);
 /* The ensemble's CUDA stream (a cudaStream_t; its blocks run on it). */
