@@ -518,10 +518,11 @@ __device__ __forceinline__ DriftInvariants drift_invariants(double rx, double ry
 // the pre-solve for drifts inside its training box; it runs per lane, inline
 // with a small register footprint (mlp_forward), so the lanes that take it
 // do not hold the rest of the warp to a warp-wide decision and the drift
-// keeps its registers.  When the Newton passes
-// from its guess do not converge, the classic starter is the restart, for
-// the bounded Laguerre iteration that is every starter's last resort.
-template <bool LEARNED>
+// keeps its registers (NET_ROWS, NET_QU: the network's shape, mlp_forward).
+// When the Newton passes from its guess do not converge, the classic starter
+// is the restart, for the bounded Laguerre iteration that is every starter's
+// last resort.
+template <bool LEARNED, int NET_ROWS = MLP_ROWS, int NET_QU = 1>
 __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, double& rz, double& vx, double& vy, double& vz,
                                                    double& r2_io, double& rinv_io, const DriftInvariants& q, double dt,
                                                    double mu, int starter, const MlpDev* mlp, double tol_dt)
@@ -537,7 +538,7 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
     res.wide = starter != STARTER_CLASSIC && !series;
     double s = -1.0;
     if constexpr (LEARNED) {
-        if (res.wide) s = starter_learned(mlp, T, rinv, q.tau2, u, mu_r, alpha);
+        if (res.wide) s = starter_learned<NET_ROWS, NET_QU>(mlp, T, rinv, q.tau2, u, mu_r, alpha);
     }
     const bool net = s > 0;     // -1 outside the training box (NaN fails too)
     if (!net) {

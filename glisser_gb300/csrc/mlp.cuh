@@ -83,13 +83,17 @@ __device__ __forceinline__ float mlp_sigmoid(float a) { return __fdividef(1.0f, 
 // given up for it.
 // Weight rows are read with 16-byte loads; every thread of a warp reads the
 // same address, so each load is one broadcast transaction.
-// Rows of the hidden layer computed together: each activation read from
-// thread-local memory serves MLP_ROWS rows, and the rows' FMA chains are
+// The hidden layer is computed ROWS rows at a time: each activation read
+// from thread-local memory serves ROWS rows, and the rows' FMA chains are
 // independent, so the network's latency (it holds up the warp it runs in)
-// is a fraction of a row-at-a-time loop's.  Each row's sum keeps the order
-// of the training kernels' forward pass.
+// is a fraction of a row-at-a-time loop's; QU activation reads per row group
+// are in flight at once.  Each row's sum keeps the order of the training
+// kernels' forward pass, so neither changes the result, only the registers
+// and the latency: the single-system learned kernel, whose register budget
+// has room, unrolls further than the ensemble kernel.
 constexpr int MLP_ROWS = 4;
 
+template <int ROWS = MLP_ROWS, int QU = 1>
 __device__ __forceinline__ float mlp_forward(const MlpDev* __restrict__ w, float x0, float x1, float x2)
 {
     x0 = bf16_split_sum(x0);
@@ -113,15 +117,15 @@ __device__ __forceinline__ float mlp_forward(const MlpDev* __restrict__ w, float
     }
     float y = __ldg(&w->b3);
 #pragma unroll 1
-    for (int j = 0; j < MLP_H; j += MLP_ROWS) {
-        float a[MLP_ROWS];
+    for (int j = 0; j < MLP_H; j += ROWS) {
+        float a[ROWS];
 #pragma unroll
-        for (int k = 0; k < MLP_ROWS; k++) a[k] = __ldg(&w->b2[j + k]);
-#pragma unroll 1
+        for (int k = 0; k < ROWS; k++) a[k] = __ldg(&w->b2[j + k]);
+#pragma unroll QU
         for (int q = 0; q < MLP_H / 4; q++) {
             const float4 h = h1[q];
 #pragma unroll
-            for (int k = 0; k < MLP_ROWS; k++) {
+            for (int k = 0; k < ROWS; k++) {
                 const float4 r = __ldg(reinterpret_cast<const float4*>(w->w2[j + k]) + q);
                 a[k] = fmaf(r.x, h.x, a[k]);
                 a[k] = fmaf(r.y, h.y, a[k]);
@@ -130,7 +134,7 @@ __device__ __forceinline__ float mlp_forward(const MlpDev* __restrict__ w, float
             }
         }
 #pragma unroll
-        for (int k = 0; k < MLP_ROWS; k++) y = fmaf(__ldg(&w->w3[j + k]), a[k] * mlp_sigmoid(a[k]), y);
+        for (int k = 0; k < ROWS; k++) y = fmaf(__ldg(&w->w3[j + k]), a[k] * mlp_sigmoid(a[k]), y);
     }
     return y;
 }
@@ -172,13 +176,15 @@ __device__ __forceinline__ double learned_guess(const MlpDev* __restrict__ w, do
     return T * f64_of_f32(__expf(z * sqrtf(tau2)));
 }
 
-// Learned guess for s, or -1 when the drift is outside the training box.
+// Learned guess for s, or -1 when the drift is outside the training box
+// (ROWS, QU: mlp_forward's shape).
+template <int ROWS = MLP_ROWS, int QU = 1>
 __device__ __forceinline__ double starter_learned(const MlpDev* __restrict__ w, double T, double rinv, float tau2,
                                                   double u, double mu_r, double alpha)
 {
     float x0, x1, x2;
     if (!mlp_inputs(w, tau2, u, rinv, mu_r, alpha, x0, x1, x2)) return -1.0;
-    return learned_guess(w, T, tau2, mlp_forward(w, x0, x1, x2));
+    return learned_guess(w, T, tau2, mlp_forward<ROWS, QU>(w, x0, x1, x2));
 }
 
 }  // namespace glisser

@@ -181,7 +181,7 @@ __device__ __forceinline__ void planet_kick64(const double* L, int j, double rx,
 // thread; carried across tiles of a persistent CTA).  Returns false after a
 // staging timeout.  KICK64: the planet kick and its radius tests in FP64
 // (planet_kick64) instead of float-float.
-template <int NP, int CTA, int PPT, bool LEARNED, bool KICK64>
+template <int NP, int CTA, int PPT, bool LEARNED, bool KICK64, int NET_ROWS = MLP_ROWS, int NET_QU = 1>
 __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uint32_t first, uint32_t count,
                                          double* stage, CtaShared& sh, uint32_t* phase)
 {
@@ -268,8 +268,9 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
                 if (flags[k] != 0) continue;
                 const DriftInvariants q =
                     drift_invariants(rx[k], ry[k], rz[k], vx[k], vy[k], vz[k], r2[k], rinv[k], p.dt, mu);
-                DriftResult d = kepler_drift<LEARNED>(rx[k], ry[k], rz[k], vx[k], vy[k], vz[k], r2[k], rinv[k], q,
-                                                       p.dt, mu, p.starter, p.mlp, p.tol_dt);
+                DriftResult d = kepler_drift<LEARNED, NET_ROWS, NET_QU>(rx[k], ry[k], rz[k], vx[k], vy[k], vz[k], r2[k],
+                                                                         rinv[k], q, p.dt, mu, p.starter, p.mlp,
+                                                                         p.tol_dt);
                 uint16_t fl = d.flags;
                 evals += d.evals;
                 if constexpr (LEARNED) nets += d.net;

@@ -27,6 +27,15 @@ using namespace tile;
 #define GLISSER_TB_MIN_BLOCKS_LEARNED GLISSER_TB_MIN_BLOCKS
 #endif
 
+// The network's shape in the learned kernel (mlp_forward: rows of the
+// hidden layer per pass, activation reads in flight): with the single-system
+// kernel's register budget (96 at 10 CTAs of 64) the network fits unrolled
+// without spills; four rows with four reads in flight, eight rows with one
+// and four rows with two measured within 0.2 % of each other on the
+// scattered disk, 0.9 % faster than four rows with one.
+constexpr int TB_NET_ROWS = 4;
+constexpr int TB_NET_QU = 4;
+
 // Particles per thread of the plain-starter kernel (a build-time tuning
 // knob; the learned kernel keeps one).  Two (118 registers, 8 CTAs per SM)
 // measured 14 % slower on the plain-giants workload and 36 % on the
@@ -48,8 +57,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS, LEARNED ? GLISSER_TB_MIN_BLOCKS
     uint32_t phase[2] = { 0, 0 };
     constexpr int PPT = LEARNED ? 1 : GLISSER_TB_PPT;
     const uint32_t first = blockIdx.x * (uint32_t)(BLOCK_THREADS * PPT);
-    run_tile<NP, BLOCK_THREADS, PPT, LEARNED, KICK64>(p, log, first, min((uint32_t)(BLOCK_THREADS * PPT), n - first),
-                                                      stage, sh, phase);
+    run_tile<NP, BLOCK_THREADS, PPT, LEARNED, KICK64, TB_NET_ROWS, TB_NET_QU>(
+        p, log, first, min((uint32_t)(BLOCK_THREADS * PPT), n - first), stage, sh, phase);
 }
 
 template <int NP, bool LEARNED, bool KICK64>
