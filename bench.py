@@ -879,8 +879,9 @@ def main():
     ap.add_argument("--ensemble-shape", default="", help="T,cta,ppt: skip the autotuner")
     ap.add_argument("--plain-systems", type=int, default=0, help="systems run one at a time (0: all)")
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--sample-particles", type=int, default=65536)
-    ap.add_argument("--sample-steps", type=int, default=256)
+    # the CPU sample: ~5.4e8 particle-steps, 7-8 s on the GPU host's 16 cores
+    ap.add_argument("--sample-particles", type=int, default=524288)
+    ap.add_argument("--sample-steps", type=int, default=1024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-oracle", action="store_true")
     ap.add_argument("--particles", type=int, default=1_000_000)

@@ -18,23 +18,23 @@ using namespace tile;
 #define GLISSER_TB_MIN_BLOCKS 10
 #endif
 
-// The learned-starter kernel runs the network per lane, as an out-of-line
-// call, only where the series starter is outside its domain; it is held to
-// the plain kernel's occupancy, so that the registers the network needs on
-// top of the drift's are saved around that call instead of lowering the
-// occupancy of every step.
+// The learned-starter kernel runs the network per lane, inline, only where
+// the series starter is outside its domain.  Its register allocation is held
+// to the plain kernel's 80 (12 CTAs' worth; shared memory admits 11 of
+// either), so that the network costs no occupancy on the steps that do not
+// run it: at 96 registers (10 CTAs) the kernel ran 4 % behind the plain one
+// on the scattered disk even with the network switched off, the drifts it
+// would start taking the FP32 pre-solve.  The network's shape (mlp_forward:
+// rows of the hidden layer per pass, activation reads in flight) is chosen
+// within that budget: four rows with two reads in flight measured 0.996 of
+// the plain kernel on the scattered disk and 1.13 on the close-eccentric
+// workload, against 0.989 and 1.12 with one read in flight and, at 96
+// registers, 0.986 and 1.08 with four.
 #ifndef GLISSER_TB_MIN_BLOCKS_LEARNED
-#define GLISSER_TB_MIN_BLOCKS_LEARNED GLISSER_TB_MIN_BLOCKS
+#define GLISSER_TB_MIN_BLOCKS_LEARNED 12
 #endif
-
-// The network's shape in the learned kernel (mlp_forward: rows of the
-// hidden layer per pass, activation reads in flight): with the single-system
-// kernel's register budget (96 at 10 CTAs of 64) the network fits unrolled
-// without spills; four rows with four reads in flight, eight rows with one
-// and four rows with two measured within 0.2 % of each other on the
-// scattered disk, 0.9 % faster than four rows with one.
 constexpr int TB_NET_ROWS = 4;
-constexpr int TB_NET_QU = 4;
+constexpr int TB_NET_QU = 2;
 
 // Particles per thread of the plain-starter kernel (a build-time tuning
 // knob; the learned kernel keeps one).  Two (118 registers, 8 CTAs per SM)
