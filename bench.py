@@ -60,15 +60,15 @@ ENSEMBLE_WORKLOAD = ("ensembles: 256 systems (Sun + 4 giants, masses x U(0.9,1.1
 # kernels whose rooflines the bench reports; the captures and their commands
 # are summarised under profiles/.
 FP64_COUNTS = {
-    "batched_kernel<4,128,1,series>": {"dadd": 2.0, "dfma": 33.0, "dmul": 22.0, "pipe_busy": 0.796,
+    "batched_kernel<4,128,1,series>": {"dadd": 1.0, "dfma": 26.0, "dmul": 17.0, "pipe_busy": 0.697,
                                        "profile": "profiles/batched_kernel_ensembles.md"},
-    "timeblock_kernel<4>": {"dadd": 2.0, "dfma": 31.1, "dmul": 21.1, "pipe_busy": 0.719,
+    "timeblock_kernel<4>": {"dadd": 1.0, "dfma": 26.0, "dmul": 17.0, "pipe_busy": 0.641,
                             "profile": "profiles/timeblock_kernel_plain-giants.md"},
 }
 # DRAM bytes per particle per block of the batched kernel (ncu dram__bytes_read
-# + dram__bytes_write, 150.6 + 68.7 MB, on a capture of one block of a quarter
+# + dram__bytes_write, 153.2 + 79.6 MB, on a capture of one block of a quarter
 # of the headline workload: 1,537,972 particles, T = 1024)
-DRAM_BYTES_PER_PARTICLE_BLOCK = 142.6
+DRAM_BYTES_PER_PARTICLE_BLOCK = 151.4
 
 
 def alg_flops_per_particle_step(n_planets, k_ref=5):

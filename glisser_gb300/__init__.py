@@ -144,6 +144,7 @@ def lib():
             "glisser_elements_to_cartesian": ([C.c_size_t, C.c_double, D, D, D], C.c_int),
             "glisser_fp64_peak_probe": ([D, D], C.c_int),
             "glisser_fastmath_check": ([C.c_size_t, P, P, P, P, P, P, P], C.c_int),
+            "glisser_drift_math_check": ([C.c_size_t, P, P, P, P, P, P, P, P, P], C.c_int),
             "glisser_launches": ([P, C.POINTER(C.c_ulonglong)], C.c_int),
             "glisser_l2_flush": ([P, C.c_size_t], C.c_int),
             "glisser_wait_check": ([C.c_double, U32, D], C.c_int),
@@ -274,6 +275,27 @@ def fastmath_check(hi, lo, d, c):
         _raise(rc, last_error())
     torch.cuda.synchronize()
     return out[0].cpu().numpy(), out[1].cpu().numpy()
+
+
+def drift_math_check(x, s, alpha, tau2):
+    """The drift's reciprocal square root and Stumpff evaluation on cuda:0,
+    elementwise over host arrays: returns 1/sqrt(x) and G1, G2, G3 at
+    (s, alpha), the float-float tier allowed where tau2 is below its bound
+    (decided per 32 consecutive elements, as a warp of the drift)."""
+    import torch
+    dev = torch.device("cuda:0")
+    t = [torch.tensor(np.ascontiguousarray(a, dt), device=dev)
+         for a, dt in ((x, np.float64), (s, np.float64), (alpha, np.float64), (tau2, np.float32))]
+    n = len(t[0])
+    if any(len(a) != n for a in t):
+        raise ValueError("drift_math_check: arrays of different lengths")
+    out = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(4)]
+    rc = lib().glisser_drift_math_check(n, *[a.data_ptr() for a in t], *[o.data_ptr() for o in out],
+                                        C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    if rc:
+        _raise(rc, last_error())
+    torch.cuda.synchronize()
+    return tuple(o.cpu().numpy() for o in out)
 
 
 def l2_flush(stream, nbytes=256 << 20):

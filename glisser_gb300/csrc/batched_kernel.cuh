@@ -10,20 +10,23 @@ namespace {
 
 using namespace tile;
 
-// Resident threads per SM the ensemble kernel's registers are sized for
-// (plain and learned starter); a build-time tuning knob.
+// Resident threads per SM the ensemble kernel's registers are sized for; a
+// build-time tuning knob.  The plain-starter kernel is latency-bound (FP64
+// pipe ~65 % busy, issue ~57 % at 5 CTAs of 128), so it is sized for 8 CTAs
+// of 128 per SM (64 registers, ~100 bytes of spills; 64-step planet-log
+// chunks fit 8 CTAs' shared memory): 6 % faster than 5 CTAs at 93
+// registers, and ahead of 6, 7 and 9 CTAs.  The learned-starter kernel keeps
+// 512 (its network's registers).
 #ifndef GLISSER_BATCHED_THREADS_PER_SM
-#define GLISSER_BATCHED_THREADS_PER_SM 512
+#define GLISSER_BATCHED_THREADS_PER_SM 1024
 #endif
 #ifndef GLISSER_BATCHED_THREADS_PER_SM_LEARNED
-#define GLISSER_BATCHED_THREADS_PER_SM_LEARNED GLISSER_BATCHED_THREADS_PER_SM
+#define GLISSER_BATCHED_THREADS_PER_SM_LEARNED 512
 #endif
 
-// Persistent kernel over (system, tile) work items.  Register budget: 128
-// per thread (512 resident threads per SM).  The learned starter runs its
-// network per lane, as an out-of-line call, only where the series starter is
-// outside its domain, and is held to the same budget (what the network needs
-// beyond it is saved around that call).
+// Persistent kernel over (system, tile) work items.  The learned starter
+// runs its network per lane, inline, only where the series starter is
+// outside its domain.
 template <int NP, int CTA, int PPT, bool LEARNED, bool KICK64>
 __global__ void __launch_bounds__(CTA, (LEARNED ? GLISSER_BATCHED_THREADS_PER_SM_LEARNED
                                                 : GLISSER_BATCHED_THREADS_PER_SM) / CTA)

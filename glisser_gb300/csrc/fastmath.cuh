@@ -11,6 +11,9 @@
 //   rcp:   e = 1 - x y,    y' = y (1 + e + e^2)           (3 FP64 ops)
 // the residual error is O(e^3) ~ 1e-20, below double rounding.  Arguments
 // outside the normal float range (and NaN/inf) take the library routines.
+// The drift's own 1/|r| (rsqrt_lean, below the float-float arithmetic) keeps
+// only the residual e in FP64 and applies the correction in float-float: one
+// FP64 instruction instead of five.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -174,10 +177,13 @@ __device__ __forceinline__ bool ff_lt(ff a, ff b) { return a.hi < b.hi || (a.hi 
 
 __device__ __forceinline__ ff ff_scale(ff a, float pow2) { return { a.hi * pow2, a.lo * pow2 }; }   // exact
 
-// 1/6 and 1/12 as float-floats (hi the nearest float, lo the nearest float
-// to the remainder: 8e-16 relative)
+// 1/6, 1/12, -1/24, -1/120 and 1/720 as float-floats (hi the nearest float, lo
+// the nearest float to the remainder: within 1.1e-15 relative)
 __device__ __forceinline__ ff ff_sixth() { return { 1.0f / 6.0f, -4.9670538e-09f }; }
 __device__ __forceinline__ ff ff_twelfth() { return { 1.0f / 12.0f, -2.4835269e-09f }; }
+__device__ __forceinline__ ff ff_neg_24th() { return { -1.0f / 24.0f, 1.2417635e-09f }; }
+__device__ __forceinline__ ff ff_neg_120th() { return { -1.0f / 120.0f, 4.346172e-10f }; }
+__device__ __forceinline__ ff ff_720th() { return { 1.0f / 720.0f, -3.3631094e-11f }; }
 __device__ __forceinline__ ff ff_neg(ff a) { return { -a.hi, -a.lo }; }
 
 // A double as a float-float on the integer pipe: hi = d rounded toward zero
@@ -241,6 +247,35 @@ __device__ __forceinline__ double f64_add_tiny(double d, float c)
     return __longlong_as_double(r);
 }
 
+// 1/sqrt(x) to FP64 accuracy (within about one unit in the last place) with
+// a single FP64 instruction, for the drift's 1/|r|.  The FP32 seed y (MUFU,
+// |e| < 2^-21 below); y^2, which a float product and its FMA error hold
+// exactly, moved into a double on the integer pipe; the residual
+// e = 1 - x y^2 by one FP64 FMA (the product exact inside it, one rounding
+// of a 2^-21-sized result: e is exact to ~2^-74); then the third-order
+// correction y (1 + e/2 + 3e^2/8) as y + y c with c = e/2 + 3e^2/8 in
+// float-float (~2^-47 of c, itself ~2^-22 of y): y + c y.hi is split by an
+// exact two-sum whose pair moves into a double exactly (ff_to_f64), and the
+// remaining c y.lo (~2^-46 of y) is added on the integer pipe
+// (f64_add_tiny).  The dropped 5e^3/16 term is below 2^-64.  rsqrt_fast,
+// the same correction in FP64 throughout, takes 5 FP64 instructions.
+// Domain: 2^-124 <= x < 2^67, where y^2 (down to 2^-67) moves into a double
+// on the integer pipe with both halves normal floats; other arguments take
+// rsqrt_fast.
+__device__ __forceinline__ double rsqrt_lean(double x)
+{
+    const int hi = __double2hiint(x);
+    if ((unsigned)(((hi >> 20) & 0x7FF) - (1023 - 124)) >= 191u || hi < 0) return rsqrt_fast(x);
+    const float y = rsqrtf(seed_float(hi));
+    const ff y2 = ff_two_prod(y, y);
+    const double e = fma(-x, ff_to_f64(y2), 1.0);
+    const ff ef = ff_split(e);
+    const ff c = ff_add_f(ff_scale(ef, 0.5f), 0.375f * ef.hi * ef.hi);
+    const ff yc = ff_mul_f(c, y);
+    const ff s = ff_two_sum(y, yc.hi);
+    return f64_add_tiny(ff_to_f64(s), yc.lo);
+}
+
 // m x^(-3/2) for float-float x = |dr|^2 and m (a planet's pull, as
 // pull_factor), on the FP32 pipe: the seed y = rsqrtf(x.hi), e = 1 - x y^2
 // with x y^2 in float-float (y^2 is exact), and the correction
@@ -263,6 +298,15 @@ __device__ __forceinline__ ff pull_factor_ff(ff x, ff m, double m15)
     const float c = __fmul_rn(e, __fmaf_rn(1.875f, e, 1.5f));
     const ff my3 = ff_mul(m, ff_mul_f(y2, y));
     return ff_add_f(my3, __fmul_rn(my3.hi, c));
+}
+
+// d / 2, exact, on the integer pipe (the exponent field lowered by one) for
+// normal d whose half is normal too; other d take the FP64 multiply.
+__device__ __forceinline__ double f64_half(double d)
+{
+    const long long b = __double_as_longlong(d);
+    const unsigned e = (unsigned)((unsigned long long)b >> 52) & 0x7FFu;
+    return (e - 2u < 0x7FDu) ? __longlong_as_double(b - (1ll << 52)) : d * 0.5;
 }
 
 // a < b for a >= +0 (or NaN) and finite b >= +0, on the integer pipe: the

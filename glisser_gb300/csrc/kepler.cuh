@@ -58,6 +58,12 @@ enum Starter : int {
     STARTER_LEARNED = 2,   // series where it applies, else the MLP over drift invariants; classic restart
 };
 
+// tau^2 = dt^2 mu / r0^3 below which the tenth-order series starter is used
+// (further down), and below which the Stumpff evaluation may take its
+// float-float tier (gfuns: mu G3 / dt ~ tau^2 / 6 stays below 3.4e-4 there).
+constexpr float SERIES_TAU2_MAX = 0.01f;
+constexpr float SMALL_STEP_TAU2 = 2e-3f;
+
 // G1, G2, G3 of one Stumpff evaluation; G0 = 1 - alpha G2 is formed where a
 // pass needs it (gfun_g0), in FP64 or FP32.
 struct GFun {
@@ -94,31 +100,45 @@ __device__ __forceinline__ void stumpff_short(double x, double& c2, double& c3)
 // The time-block kernels are bound by the FP64 pipe, so here and in the
 // solver below float-to-double sums and the residual-accepted fold go through
 // the integer pipe (ff_to_f64, f64_add_tiny).
-__device__ __forceinline__ GFun gfuns(double s, double alpha)
+__device__ __forceinline__ GFun gfuns(double s, double alpha, bool small_step)
 {
-    double s2 = s * s;
-    double x = alpha * s2;
+    const double s2 = s * s;
     double c2, c3;
     GFun g;
-    const double ax = fabs(x);
+    // x = alpha s^2 in float-float (~2^-46): the float-float tier below needs
+    // no more, and its high part decides the tier (formed for every lane:
+    // predicating it on the step size measured 1-2 % slower)
+    const ff sf = ff_split(s);
+    const ff s2f = ff_sqr(sf);
+    const ff xff = ff_mul(ff_split(alpha), s2f);
     const unsigned lanes = __activemask();
-    if (__all_sync(lanes, lt_nonneg(ax, 1e-4))) {
-        // warp-uniform: every lane in this pass has a tiny argument (steps of
-        // a few thousandths of an orbit).  G3 = s^3 c3 enters Kepler's
-        // equation, the g function and G1 only as mu G3 / dt ~ tau^2 / 6 or
-        // alpha G3 / s = x c3, both below ~3e-5 here, so it is formed in
-        // float-float on the FP32 pipe (c3's x terms in FP32, 3e-13 of c3)
-        c2 = fma(x, fma(x, 1.0 / 720.0, -1.0 / 24.0), 0.5);
-        const ff sf = ff_split(s);
-        const float xf = f32_trunc(x);
-        const ff c3f = ff_add_f(ff_sixth(), xf * fmaf(xf, 1.0f / 5040.0f, -1.0f / 120.0f));
-        const ff g3f = ff_mul(ff_mul(sf, ff_sqr(sf)), c3f);
-        g.g2 = s2 * c2;
+    if (__all_sync(lanes, small_step && fabsf(xff.hi) < 2e-3f)) {
+        // warp-uniform: every lane in this pass has a small argument and a
+        // small step (tau^2 < SMALL_STEP_TAU2).  G2 = s^2 (1/2 + d) with
+        // d = x (-1/24 + x/720 - x^2/40320), |d| < 8.4e-5: d is needed to
+        // ~2^-41 of itself, so it is formed in float-float (x/720 too; the
+        // x^2 term in FP32) and G2 takes one FP64 FMA; the dropped x^4 term is
+        // below 1e-17 of c2.  G3 = s^3 c3 enters Kepler's equation and the g
+        // function as mu G3 / dt ~ tau^2 / 6 < 3.4e-4 and G1 as
+        // alpha G3 / s = x c3 < 3.4e-4, so ~2^-41 of G3 suffices too: c3's x
+        // term in float-float, its x^2 and x^3 terms in FP32, the product in
+        // float-float
+        const float xf = xff.hi;
+        const ff in2 = ff_add_f(ff_add(ff_neg_24th(), ff_mul(xff, ff_720th())), (xf * xf) * (-1.0f / 40320.0f));
+        const ff d = ff_mul(xff, in2);
+        const ff in3 = ff_add_f(ff_neg_120th(), xf * fmaf(xf, -1.0f / 362880.0f, 1.0f / 5040.0f));
+        const ff c3f = ff_add(ff_sixth(), ff_mul(xff, in3));
+        const ff g3f = ff_mul(ff_mul(sf, s2f), c3f);
+        g.g2 = fma(s2, ff_to_f64(d), f64_half(s2));
         g.g3 = ff_to_f64(g3f);
         g.g1 = fma(-alpha, g.g3, s);
         return g;
-    } else if (__all_sync(lanes, lt_nonneg(ax, 2e-3))) {
-        // warp-uniform: every lane in this pass has a small argument
+    }
+    double x = alpha * s2;
+    const double ax = fabs(x);
+    if (__all_sync(lanes, lt_nonneg(ax, 2e-3))) {
+        // warp-uniform: every lane in this pass has a small argument (and
+        // some lane a step too large for the float-float tier)
         stumpff_short(x, c2, c3);
     } else if (fabs(x) < 0.1) {
         stumpff_small(x, c2, c3);
@@ -245,7 +265,6 @@ __device__ __forceinline__ double starter_fp32_kepler(double dt, double r0, doub
 // first Stumpff evaluation; orders 8-10 keep that true for eccentric orbits
 // near pericentre (tau^2 up to SERIES_TAU2_MAX).  Orders 2-4 are summed in
 // FP64, orders 5-10 (below 1e-9 of s) in FP32.
-constexpr float SERIES_TAU2_MAX = 0.01f;
 
 // tau^2 = (dt / r0)^2 (mu / r0), the step over the local dynamical time
 // squared, in FP32 on the integer and FP32 pipes: it only chooses the
@@ -423,10 +442,10 @@ __device__ __forceinline__ void fold_small(GFun& g, double& ds, double f, double
 //       G1 + ds (G0 - alpha ds/2 (G1 + ds/3 G0));
 //     the dropped terms are below ~(ds/s)^4 ~ 1e-16 of G.
 __device__ __forceinline__ bool kepler_newton(double& s, double dt, double r0, double u, double mu, double alpha,
-                                              double tol, GFun& g, double& ds, uint16_t& evals)
+                                              double tol, bool small_step, GFun& g, double& ds, uint16_t& evals)
 {
     for (int it = 0; it < KEP_NEWTON_MAX; it++) {
-        g = gfuns(s, alpha);
+        g = gfuns(s, alpha, small_step);
         evals++;
         double f = fma(r0, g.g1, fma(u, g.g2, fma(mu, g.g3, -dt)));
         if (lt_nonneg(fabs(f), tol)) {
@@ -466,7 +485,7 @@ __device__ __forceinline__ bool kepler_laguerre(double& s, double dt, double r0,
     const double ln = 5.0;
     const double k = fma(-alpha, r0, mu);
     for (int it = 0; it < KEP_LAGUERRE_MAX; it++) {
-        g = gfuns(s, alpha);
+        g = gfuns(s, alpha, false);
         evals++;
         const double g0 = gfun_g0(g, alpha);
         double f = fma(r0, g.g1, fma(u, g.g2, fma(mu, g.g3, -dt)));
@@ -549,7 +568,7 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
     const double tol = tol_dt;
     GFun g;
     double ds = 0;
-    bool ok = kepler_newton(s, dt, r0, u, mu, alpha, tol, g, ds, res.evals);
+    bool ok = kepler_newton(s, dt, r0, u, mu, alpha, tol, q.tau2 < SMALL_STEP_TAU2, g, ds, res.evals);
     if constexpr (LEARNED) {
         // a network guess whose Newton passes did not converge: the
         // classic starter, then the bounded Laguerre iteration from it
@@ -565,7 +584,7 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
     double gg = fma(-mu, g3, dt);
     double nrx = fma(ff, rx, gg * vx), nry = fma(ff, ry, gg * vy), nrz = fma(ff, rz, gg * vz);
     const double nr2 = fma(nrx, nrx, fma(nry, nry, nrz * nrz));
-    const double nrinv = rsqrt_fast(nr2);
+    const double nrinv = rsqrt_lean(nr2);
     double fd = -mu_r * g1 * nrinv;
     double gd = fma(-mu * g2, nrinv, 1.0);
     double nvx = fma(fd, rx, gd * vx), nvy = fma(fd, ry, gd * vy), nvz = fma(fd, rz, gd * vz);

@@ -65,7 +65,7 @@ __global__ void log_solves_kernel(glisser_particles pa, uint32_t n, double dt, d
         const double r2 = fma(rx, rx, fma(ry, ry, rz * rz));
         const double v2 = fma(vx, vx, fma(vy, vy, vz * vz));
         const double u = fma(rx, vx, fma(ry, vy, rz * vz));
-        const double rinv = rsqrt_fast(r2);
+        const double rinv = rsqrt_lean(r2);
         const double r0 = r2 * rinv;
         const double mu_r = mu * rinv;
         const double alpha = fma(2.0, mu_r, -v2);
@@ -76,7 +76,7 @@ __global__ void log_solves_kernel(glisser_particles pa, uint32_t n, double dt, d
         GFun g;
         double ds = 0;
         uint16_t ev = 0;
-        bool ok = kepler_newton(s, dt, r0, u, mu, alpha, tol, g, ds, ev);
+        bool ok = kepler_newton(s, dt, r0, u, mu, alpha, tol, tau2_f32(dt * rinv, mu_r) < SMALL_STEP_TAU2, g, ds, ev);
         if (!ok) ok = kepler_laguerre(s, dt, r0, u, mu, alpha, tol, g, ds, ev);
         float f0, f1, f2;
         mlp_features(tau2_f32(dt * rinv, mu_r), u, rinv, mu_r, alpha, f0, f1, f2);
@@ -315,7 +315,7 @@ __global__ void drift_states_kernel(glisser_particles pa, uint32_t n, double dt,
     if (i >= n) return;
     double rx = pa.rx[i], ry = pa.ry[i], rz = pa.rz[i], vx = pa.vx[i], vy = pa.vy[i], vz = pa.vz[i];
     const double r2 = fma(rx, rx, fma(ry, ry, rz * rz));
-    double r2v = r2, rinv = rsqrt_fast(r2);
+    double r2v = r2, rinv = rsqrt_lean(r2);
     DriftResult d = kepler_drift<LEARNED>(rx, ry, rz, vx, vy, vz, r2v, rinv, dt, mu, starter, mlp, KEP_TOL * dt);
     pa.rx[i] = rx; pa.ry[i] = ry; pa.rz[i] = rz;
     pa.vx[i] = vx; pa.vy[i] = vy; pa.vz[i] = vz;

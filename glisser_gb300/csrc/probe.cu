@@ -13,6 +13,7 @@
 
 #include "../../include/glisser.h"
 #include "fastmath.cuh"
+#include "kepler.cuh"
 
 namespace glisser {
 
@@ -26,6 +27,22 @@ __global__ void fastmath_check_kernel(size_t n, const float* hi, const float* lo
     if (i >= n) return;
     out_ff[i] = ff_to_f64(ff{ hi[i], lo[i] });
     out_tiny[i] = f64_add_tiny(d[i], c[i]);
+}
+
+// The drift's reciprocal square root and Stumpff evaluation on device arrays:
+// rsq[i] = rsqrt_lean(x[i]); G1, G2, G3 of gfuns(s[i], alpha[i]) with the
+// float-float tier allowed where tau2[i] < SMALL_STEP_TAU2 (the tier is
+// decided per warp, as in the drift).
+__global__ void drift_math_check_kernel(size_t n, const double* x, const double* s, const double* alpha,
+                                        const float* tau2, double* rsq, double* g1, double* g2, double* g3)
+{
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    rsq[i] = rsqrt_lean(x[i]);
+    const GFun g = gfuns(s[i], alpha[i], tau2[i] < SMALL_STEP_TAU2);
+    g1[i] = g.g1;
+    g2[i] = g.g2;
+    g3[i] = g.g3;
 }
 
 __global__ void __launch_bounds__(256) dfma_chains(double* out, int iters, double a, double b)
@@ -103,5 +120,19 @@ extern "C" int glisser_fastmath_check(size_t n, const float* hi, const float* lo
     const unsigned blocks = (unsigned)((n + threads - 1) / threads);
     if ((size_t)blocks * threads < n) return GLISSER_E_INVALID;
     glisser::fastmath_check_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(n, hi, lo, d, c, out_ff, out_tiny);
+    return cudaGetLastError() == cudaSuccess ? GLISSER_OK : GLISSER_E_CUDA;
+}
+
+extern "C" int glisser_drift_math_check(size_t n, const double* x, const double* s, const double* alpha,
+                                        const float* tau2, double* rsq, double* g1, double* g2, double* g3,
+                                        void* stream)
+{
+    if (n == 0) return GLISSER_OK;
+    if (!x || !s || !alpha || !tau2 || !rsq || !g1 || !g2 || !g3) return GLISSER_E_INVALID;
+    const unsigned threads = 256;
+    const unsigned blocks = (unsigned)((n + threads - 1) / threads);
+    if ((size_t)blocks * threads < n) return GLISSER_E_INVALID;
+    glisser::drift_math_check_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(n, x, s, alpha, tau2, rsq, g1,
+                                                                                   g2, g3);
     return cudaGetLastError() == cudaSuccess ? GLISSER_OK : GLISSER_E_CUDA;
 }

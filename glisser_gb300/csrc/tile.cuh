@@ -196,7 +196,10 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
         if (nchunks > 1) { issue_chunk(p, log, stage + bufstride, &sh.bar[1], 1, rec); inflight1 = true; }
     }
 
-    double rx[PPT], ry[PPT], rz[PPT], vx[PPT], vy[PPT], vz[PPT], ax[PPT], ay[PPT], az[PPT], r2[PPT], rinv[PPT];
+    // the acceleration is not carried between steps: each step's is used at
+    // once for the merged kick, and the last one a particle reaches (flagged
+    // or at the block's end) is stored at that step
+    double rx[PPT], ry[PPT], rz[PPT], vx[PPT], vy[PPT], vz[PPT], r2[PPT], rinv[PPT];
     uint16_t flags[PPT], flags0[PPT];
     uint32_t dti[PPT];
     uint32_t evals = 0, border = 0, nets = 0, wide = 0;
@@ -207,12 +210,13 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
     for (int k = 0; k < PPT; k++) {
         const uint32_t off = (uint32_t)k * CTA + tid;
         const uint32_t i = first + off;
-        rx[k] = ry[k] = rz[k] = vx[k] = vy[k] = vz[k] = ax[k] = ay[k] = az[k] = 0;
+        rx[k] = ry[k] = rz[k] = vx[k] = vy[k] = vz[k] = 0;
+        double a0x = 0, a0y = 0, a0z = 0;
         flags[k] = 0xFFFF;
         if (off < count) {
             rx[k] = p.pa.rx[i]; ry[k] = p.pa.ry[i]; rz[k] = p.pa.rz[i];
             vx[k] = p.pa.vx[i]; vy[k] = p.pa.vy[i]; vz[k] = p.pa.vz[i];
-            ax[k] = p.pa.ax[i]; ay[k] = p.pa.ay[i]; az[k] = p.pa.az[i];
+            a0x = p.pa.ax[i]; a0y = p.pa.ay[i]; a0z = p.pa.az[i];
             flags[k] = p.pa.flags[i];
         }
         flags0[k] = flags[k];
@@ -224,12 +228,12 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
         // 1/|r| of the position it produces: the Sun/outer test's and the next
         // drift's.
         if (flags[k] == 0 && p.len > 0) {
-            vx[k] = fma(ax[k], hdt, vx[k]);
-            vy[k] = fma(ay[k], hdt, vy[k]);
-            vz[k] = fma(az[k], hdt, vz[k]);
+            vx[k] = fma(a0x, hdt, vx[k]);
+            vy[k] = fma(a0y, hdt, vy[k]);
+            vz[k] = fma(a0z, hdt, vz[k]);
         }
         r2[k] = fma(rx[k], rx[k], fma(ry[k], ry[k], rz[k] * rz[k]));
-        rinv[k] = rsqrt_fast(r2[k]);
+        rinv[k] = rsqrt_lean(r2[k]);
     }
 
     bool ok = true;
@@ -307,9 +311,13 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
                 if (lt_nonneg(rr, rh2_sun)) fl = 0x0001;
                 if (gt_nonneg(rr, p.outer2)) fl = 0x0002;
                 flags[k] = fl;
-                ax[k] = aax; ay[k] = aay; az[k] = aaz;
                 dti[k] = cfirst + s + 1;
-                const double kc = (fl != 0 || dti[k] == p.len) ? hdt : p.dt;
+                const bool last = fl != 0 || dti[k] == p.len;
+                if (last) {
+                    const uint32_t i = first + (uint32_t)k * CTA + tid;
+                    p.pa.ax[i] = aax; p.pa.ay[i] = aay; p.pa.az[i] = aaz;
+                }
+                const double kc = last ? hdt : p.dt;
                 vx[k] = fma(aax, kc, vx[k]);
                 vy[k] = fma(aay, kc, vy[k]);
                 vz[k] = fma(aaz, kc, vz[k]);
@@ -346,7 +354,6 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
                 p.pa.rx[i] = rx[k]; p.pa.ry[i] = ry[k]; p.pa.rz[i] = rz[k];
                 p.pa.vx[i] = vx[k]; p.pa.vy[i] = vy[k]; p.pa.vz[i] = vz[k];
             }
-            p.pa.ax[i] = ax[k]; p.pa.ay[i] = ay[k]; p.pa.az[i] = az[k];
             p.pa.flags[i] = flags[k];
             p.pa.deathtime_index[i] = dti[k];
         }

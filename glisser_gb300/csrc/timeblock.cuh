@@ -10,16 +10,18 @@
 namespace glisser {
 
 // Steps per planet-log chunk staged in shared memory (even, so that every
-// chunk is a multiple of 16 bytes for the bulk copy).
+// chunk is a multiple of 16 bytes for the bulk copy).  Two chunk buffers per
+// CTA: 32 steps keep the single-system kernel's 16 CTAs of 64 within shared
+// memory with four planets (10.9 KB per CTA).
 #ifndef GLISSER_LOG_CHUNK
-#define GLISSER_LOG_CHUNK 64
+#define GLISSER_LOG_CHUNK 32
 #endif
 constexpr int LOG_CHUNK = GLISSER_LOG_CHUNK;
-// The ensemble kernel restages each system's log per tile and stays with
-// longer chunks (fewer waits per tile; it is not occupancy-limited the same
-// way).
+// The ensemble kernel restages each system's log per tile and takes longer
+// chunks (fewer waits per tile); 64 steps fit its 8 CTAs of 128 per SM
+// (18.6 KB each with four planets).
 #ifndef GLISSER_BATCH_LOG_CHUNK
-#define GLISSER_BATCH_LOG_CHUNK 128
+#define GLISSER_BATCH_LOG_CHUNK 64
 #endif
 constexpr int BATCH_LOG_CHUNK = GLISSER_BATCH_LOG_CHUNK;
 constexpr int MAX_PLANETS = 64;           // planets including the Sun

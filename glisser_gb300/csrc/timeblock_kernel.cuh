@@ -9,29 +9,29 @@ namespace {
 
 using namespace tile;
 
-// CTAs per SM the register allocation is sized for.  With the planet kick
-// and the starter in float-float on the FP32 pipe, longer dependency chains
-// make resident warps count: 10 CTAs of 64 threads (with 64-step planet-log
-// chunks, so that shared memory admits them) measured 1 % faster than 8 and
-// 12, and 4 % faster than the 7 that 128-step chunks allow.
+// CTAs per SM the register allocation is sized for.  Once the drift's
+// reciprocal square root and small-step Stumpff tier moved most of their
+// FP64 work to the FP32 and integer pipes, the kernel became latency-bound
+// with neither pipe saturated, and resident warps count: 16 CTAs of 64
+// threads (64 registers, a few dozen bytes of spills; 32-step planet-log
+// chunks, so that shared memory admits 16 with four planets) measured 7 %
+// faster than 10 CTAs at 80 registers on the plain-giants workload and 2.5 %
+// on the scattered disk; 18 and 20 CTAs spill more.
 #ifndef GLISSER_TB_MIN_BLOCKS
-#define GLISSER_TB_MIN_BLOCKS 10
+#define GLISSER_TB_MIN_BLOCKS 16
 #endif
 
 // The learned-starter kernel runs the network per lane, inline, only where
-// the series starter is outside its domain.  Its register allocation is held
-// to the plain kernel's 80 (12 CTAs' worth; shared memory admits 11 of
-// either), so that the network costs no occupancy on the steps that do not
-// run it: at 96 registers (10 CTAs) the kernel ran 4 % behind the plain one
-// on the scattered disk even with the network switched off, the drifts it
-// would start taking the FP32 pre-solve.  The network's shape (mlp_forward:
-// rows of the hidden layer per pass, activation reads in flight) is chosen
-// within that budget: four rows with two reads in flight measured 0.996 of
-// the plain kernel on the scattered disk and 1.13 on the close-eccentric
-// workload, against 0.989 and 1.12 with one read in flight and, at 96
-// registers, 0.986 and 1.08 with four.
+// the series starter is outside its domain.  Its register allocation follows
+// the plain kernel's occupancy (16 CTAs of 64 per SM: 64 registers), so that
+// the network costs no occupancy on the steps that do not run it: at 80
+// registers (12 CTAs) it ran 2.3 % behind the plain kernel on the scattered
+// disk, where 0.1 % of drifts take the network, and 2.4 % slower on the
+// close-eccentric workload, where every drift does.  The network's shape
+// (mlp_forward: four rows of the hidden layer per pass, two activation
+// reads in flight) was chosen for a register budget.
 #ifndef GLISSER_TB_MIN_BLOCKS_LEARNED
-#define GLISSER_TB_MIN_BLOCKS_LEARNED 12
+#define GLISSER_TB_MIN_BLOCKS_LEARNED 16
 #endif
 constexpr int TB_NET_ROWS = 4;
 constexpr int TB_NET_QU = 2;

@@ -444,6 +444,14 @@ int glisser_fp64_peak_probe(double *tflops, double *ms);
  * No reference counterpart. */
 int glisser_fastmath_check(size_t n, const float *hi, const float *lo, const double *d, const float *c,
                            double *out_ff, double *out_tiny, void *stream);
+/* Runs the drift's reciprocal square root and Stumpff evaluation on n device
+ * elements, for their tests: rsq[i] = 1/sqrt(x[i]) and the G-functions
+ * G1, G2, G3 at (s[i], alpha[i]), with the float-float tier that the drift
+ * takes for small steps allowed where tau2[i] (dt^2 mu / r^3) is below its
+ * bound; the tier is chosen per warp of 32 consecutive elements, as in the
+ * drift.  No reference counterpart. */
+int glisser_drift_math_check(size_t n, const double *x, const double *s, const double *alpha, const float *tau2,
+                             double *rsq, double *g1, double *g2, double *g3, void *stream);
 /* Overwrites `bytes` of a library-owned scratch buffer on `stream` (a
  * cudaStream_t) so the next kernel starts with a cold L2; benchmark hygiene,
  * no reference counterpart. */
