@@ -98,15 +98,22 @@ __device__ __forceinline__ void issue_chunk(const Common& p, const double* log, 
     bulk_copy_g2s(buf, log + (size_t)first * rec, bytes, bar);
 }
 
+// What the float-float kick reads of planet j, packed in 32 bytes so that a
+// step reads it with two 16-byte shared-memory loads instead of five.
+struct __align__(16) PlanetConst {
+    ff m;                       // m and rh^2 as float-floats
+    ff rh2;
+    double m15;                 // 1.5 m, the FP64 planet pull's form (its fallback)
+    float rh2win;               // 2^-40 rh^2: the borderline window of the float-float radius test
+    uint32_t id;
+};
+
 // Shared-memory state of one CTA.
 struct CtaShared {
     double m[MAX_PLANETS];
-    double m15[MAX_PLANETS];    // 1.5 m, the FP64 planet pull's form
     double rh2[MAX_PLANETS];
-    ff mff[MAX_PLANETS];        // m and rh^2 as float-floats for the kick
-    ff rh2ff[MAX_PLANETS];
-    float rh2win[MAX_PLANETS];  // 2^-40 rh^2: the borderline window of the float-float radius test
     uint32_t id[MAX_PLANETS];
+    PlanetConst pk[MAX_PLANETS];
     uint64_t bar[2];
     int abort;
     uint32_t item;
@@ -140,14 +147,15 @@ __device__ __forceinline__ void planet_kick(const ff* L, int j, ff rx, ff ry, ff
     const ff dy = ff_add(ry, ff_neg(L[3 * j + 1]));
     const ff dz = ff_add(rz, ff_neg(L[3 * j + 2]));
     const ff rad = ff_add(ff_add(ff_sqr(dx), ff_sqr(dy)), ff_sqr(dz));
+    const PlanetConst q = sh.pk[j];
     if (flags == 0) {
         // rad.hi - rh2.hi is exact near the threshold (Sterbenz), so the FP32
         // difference is good to a few units of the low parts
-        const float d = __fadd_rn(__fsub_rn(rad.hi, sh.rh2ff[j].hi), __fsub_rn(rad.lo, sh.rh2ff[j].lo));
-        border += fabsf(d) <= sh.rh2win[j] ? 1u : 0u;
-        if (ff_lt(rad, sh.rh2ff[j])) flags = (uint16_t)((sh.id[j] << 8) | 0x0001);
+        const float d = __fadd_rn(__fsub_rn(rad.hi, q.rh2.hi), __fsub_rn(rad.lo, q.rh2.lo));
+        border += fabsf(d) <= q.rh2win ? 1u : 0u;
+        if (ff_lt(rad, q.rh2)) flags = (uint16_t)((q.id << 8) | 0x0001);
     }
-    const ff fac = pull_factor_ff(rad, sh.mff[j], sh.m15[j]);
+    const ff fac = pull_factor_ff(rad, q.m, q.m15);
     sx = ff_add(sx, ff_mul(dx, fac));
     sy = ff_add(sy, ff_mul(dy, fac));
     sz = ff_add(sz, ff_mul(dz, fac));
@@ -200,8 +208,10 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
     // once for the merged kick, and the last one a particle reaches (flagged
     // or at the block's end) is stored at that step
     double rx[PPT], ry[PPT], rz[PPT], vx[PPT], vy[PPT], vz[PPT], r2[PPT], rinv[PPT];
-    uint16_t flags[PPT], flags0[PPT];
-    uint32_t dti[PPT];
+    // neither the block-start flags nor the deathtime index are carried:
+    // the index is stored at the particle's last step (flagged or the
+    // block's end), and the start flags are read back from memory at the end
+    uint16_t flags[PPT];
     uint32_t evals = 0, border = 0, nets = 0, wide = 0;
     const double hdt = p.dt * 0.5;
     const double mu = sh.m[0];
@@ -219,8 +229,6 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
             a0x = p.pa.ax[i]; a0y = p.pa.ay[i]; a0z = p.pa.az[i];
             flags[k] = p.pa.flags[i];
         }
-        flags0[k] = flags[k];
-        dti[k] = 0;
         // Kick-drift-kick with the two half kicks between consecutive steps
         // merged into one full kick (v += a dt); a particle takes the closing
         // half kick when it is flagged or the block ends, so its stored
@@ -311,11 +319,12 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
                 if (lt_nonneg(rr, rh2_sun)) fl = 0x0001;
                 if (gt_nonneg(rr, p.outer2)) fl = 0x0002;
                 flags[k] = fl;
-                dti[k] = cfirst + s + 1;
-                const bool last = fl != 0 || dti[k] == p.len;
+                const uint32_t step = cfirst + s + 1;
+                const bool last = fl != 0 || step == p.len;
                 if (last) {
                     const uint32_t i = first + (uint32_t)k * CTA + tid;
                     p.pa.ax[i] = aax; p.pa.ay[i] = aay; p.pa.az[i] = aaz;
+                    p.pa.deathtime_index[i] = step;
                 }
                 const double kc = last ? hdt : p.dt;
                 vx[k] = fma(aax, kc, vx[k]);
@@ -343,7 +352,12 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
         const uint32_t off = (uint32_t)k * CTA + tid;
         const uint32_t i = first + off;
         const bool active = off < count;
+        uint16_t flags0 = 0xFFFF;
+        bool ran = false;
         if (active) {
+            flags0 = p.pa.flags[i];         // the block-start flags, not yet overwritten
+            // integrated: its deathtime index was stored at its last step
+            ran = flags0 == 0 && p.len > 0;
             if (p.kill == GLISSER_ENCOUNTERS_KILL && (flags[k] & 0x01))
                 flags[k] = (uint16_t)((flags[k] & 0xFF00) | 0x80);
             // a rolled-back encounter particle leaves its block-start state in
@@ -355,10 +369,10 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
                 p.pa.vx[i] = vx[k]; p.pa.vy[i] = vy[k]; p.pa.vz[i] = vz[k];
             }
             p.pa.flags[i] = flags[k];
-            p.pa.deathtime_index[i] = dti[k];
+            if (!ran) p.pa.deathtime_index[i] = 0;
         }
         // hand-off compaction: one atomic per warp
-        const bool changed = active && flags[k] != flags0[k];
+        const bool changed = active && flags[k] != flags0;
         const unsigned ballot = __ballot_sync(0xffffffffu, changed);
         if (ballot) {
             const unsigned leader = __ffs(ballot) - 1;
@@ -371,7 +385,7 @@ __device__ __forceinline__ bool run_tile(const Common& p, const double* log, uin
                     p.ho.index[slot] = i;
                     p.ho.id[slot] = p.pa.id[i];
                     p.ho.flags[slot] = flags[k];
-                    p.ho.deathtime_index[slot] = dti[k];
+                    p.ho.deathtime_index[slot] = ran ? p.pa.deathtime_index[i] : 0u;
                 }
             }
         }
@@ -410,12 +424,15 @@ __device__ __forceinline__ void load_planet_constants(CtaShared& sh, uint32_t np
 {
     for (uint32_t j = threadIdx.x; j < npl; j += blockDim.x) {
         sh.m[j] = m[j];
-        sh.m15[j] = 1.5 * m[j];
         sh.rh2[j] = rh[j] * rh[j];
-        sh.mff[j] = ff_split(m[j]);
-        sh.rh2ff[j] = ff_split(sh.rh2[j]);
-        sh.rh2win[j] = sh.rh2ff[j].hi * 0x1p-40f;
         sh.id[j] = pid[j];
+        PlanetConst q;
+        q.m = ff_split(m[j]);
+        q.rh2 = ff_split(sh.rh2[j]);
+        q.m15 = 1.5 * m[j];
+        q.rh2win = q.rh2.hi * 0x1p-40f;
+        q.id = pid[j];
+        sh.pk[j] = q;
     }
 }
 
