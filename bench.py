@@ -256,14 +256,17 @@ def run_reference_arm(args, rank, world):
     systems = to_cartesian(O.elements_to_cartesian, ensemble_elements(0, fraction=args.ensemble_fraction))
     threads = os.cpu_count() or 1
     kind = None
+    # each step a quarter of the GPU arm's CPU sample (~1.7 s on 16 cores), so
+    # that --steps 20 --warmup 5 ends within a minute or so
+    sample = max(1, args.sample_particles // 4)
     for _ in range(args.warmup):
-        reference_cpu_rate(systems, args.sample_particles, args.sample_steps, threads)
+        reference_cpu_rate(systems, sample, args.sample_steps, threads)
     els = []
     for _ in range(args.steps):
-        _, el, kind = reference_cpu_rate(systems, args.sample_particles, args.sample_steps, threads)
+        _, el, kind = reference_cpu_rate(systems, sample, args.sample_steps, threads)
         els.append(el)
-    value = len(els) * args.sample_particles * args.sample_steps / sum(els)
-    note = cpu_sample_note(kind, args.sample_particles, args.sample_steps, threads)
+    value = len(els) * sample * args.sample_steps / sum(els)
+    note = cpu_sample_note(kind, sample, args.sample_steps, threads)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * sum(els) / len(els), "higher_is_better": True,
