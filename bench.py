@@ -60,15 +60,15 @@ ENSEMBLE_WORKLOAD = ("ensembles: 256 systems (Sun + 4 giants, masses x U(0.9,1.1
 # kernels whose rooflines the bench reports; the captures and their commands
 # are summarised under profiles/.
 FP64_COUNTS = {
-    "batched_kernel<4,128,1,series>": {"dadd": 1.0, "dfma": 26.0, "dmul": 17.0, "pipe_busy": 0.697,
+    "batched_kernel<4,128,1,series>": {"dadd": 1.0, "dfma": 26.0, "dmul": 17.0, "pipe_busy": 0.776,
                                        "profile": "profiles/batched_kernel_ensembles.md"},
-    "timeblock_kernel<4>": {"dadd": 1.0, "dfma": 26.0, "dmul": 17.0, "pipe_busy": 0.641,
+    "timeblock_kernel<4>": {"dadd": 1.0, "dfma": 26.0, "dmul": 17.0, "pipe_busy": 0.709,
                             "profile": "profiles/timeblock_kernel_plain-giants.md"},
 }
 # DRAM bytes per particle per block of the batched kernel (ncu dram__bytes_read
-# + dram__bytes_write, 153.2 + 79.6 MB, on a capture of one block of a quarter
+# + dram__bytes_write, 153.2 + 78.8 MB, on a capture of one block of a quarter
 # of the headline workload: 1,537,972 particles, T = 1024)
-DRAM_BYTES_PER_PARTICLE_BLOCK = 151.4
+DRAM_BYTES_PER_PARTICLE_BLOCK = 150.8
 
 
 def alg_flops_per_particle_step(n_planets, k_ref=5):

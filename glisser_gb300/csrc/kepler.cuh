@@ -38,7 +38,12 @@
 //    fastmath.cuh);
 //  * the Stumpff series is evaluated by Horner in x = alpha s^2; arguments
 //    with |x| >= 0.1 are quartered and rebuilt with the double-angle
-//    identities (c0,c1,c2,c3 as in Danby eq. 6.9.15).
+//    identities (c0,c1,c2,c3 as in Danby eq. 6.9.15).  For a small step
+//    (|x| < 2e-3, tau^2 < 2e-3) the corrections to G2 = s^2/2 and all of G3
+//    need far fewer than 53 bits and are formed in float-float: three FP64
+//    instructions instead of twelve;
+//  * the new 1/|r| keeps one FP64 instruction (the residual of the FP32
+//    seed), its correction in float-float (rsqrt_lean in fastmath.cuh).
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>

@@ -25,9 +25,10 @@ using namespace tile;
 // the series starter is outside its domain.  Its register allocation follows
 // the plain kernel's occupancy (16 CTAs of 64 per SM: 64 registers), so that
 // the network costs no occupancy on the steps that do not run it: at 80
-// registers (12 CTAs) it ran 2.3 % behind the plain kernel on the scattered
-// disk, where 0.1 % of drifts take the network, and 2.4 % slower on the
-// close-eccentric workload, where every drift does.  The network's shape
+// registers (12 CTAs) it ran 0.991x the plain kernel on the scattered disk,
+// where 0.1 % of drifts take the network, and 1.062x on the close-eccentric
+// workload, where every drift does; at 64 registers 1.016x and 1.071x (the
+// spills sit around the network).  The network's shape
 // (mlp_forward: four rows of the hidden layer per pass, two activation
 // reads in flight) was chosen for a register budget.
 #ifndef GLISSER_TB_MIN_BLOCKS_LEARNED
