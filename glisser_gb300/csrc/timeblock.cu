@@ -1,8 +1,9 @@
 // Particle time-block kernels: the GB300 replacement of MVSKernel
 // (src/wh.cu:15-207) and its launch (src/wh.cu:344-395).
 //
-// One thread keeps the state of its particle(s) -- r, v, a and the flag word
-// -- in registers for the whole block of `len` steps; the particle arrays are
+// One thread keeps the state of its particle(s) -- r, v and the flag word --
+// in registers for the whole block of `len` steps (the acceleration and the
+// deathtime index are stored at the particle's last step); the arrays are
 // structure-of-arrays FP64 so every load and store is a fully coalesced
 // 8-byte-per-lane access.  The planet log (per step: h0, then the planet
 // positions) is staged into shared memory in chunks of `chunk` steps by bulk
