@@ -163,8 +163,9 @@ __device__ __forceinline__ void planet_kick(const ff* L, int j, ff rx, ff ry, ff
 
 // The same kick term in FP64, as the reference computes it (src/wh.cu:142-160:
 // the FP64 squared distance compared with the FP64 rh^2, a -= m dr / |dr|^3
-// accumulated from a = h0), with |dr|^-3 from the FP64 reciprocal square root
-// (the reference's 1 / (rad sqrt(rad)) to rounding).  The build's FP64-kick
+// accumulated from a = h0), with |dr|^-3 from the FP64-accurate reciprocal
+// square root (rsqrt_lean: within about one unit in the last place, the
+// reference's 1 / (rad sqrt(rad)) to rounding).  The build's FP64-kick
 // kernels use it (GLISSER_KICK_FP64).
 __device__ __forceinline__ void planet_kick64(const double* L, int j, double rx, double ry, double rz, double& ax,
                                               double& ay, double& az, uint16_t& flags, uint32_t& border,
@@ -176,7 +177,7 @@ __device__ __forceinline__ void planet_kick64(const double* L, int j, double rx,
         border += near_nonneg(rad, sh.rh2[j]);
         if (lt_nonneg(rad, sh.rh2[j])) flags = (uint16_t)((sh.id[j] << 8) | 0x0001);
     }
-    const double y = rsqrt_fast(rad);
+    const double y = rsqrt_lean(rad);
     const double fac = sh.m[j] * (y * (y * y));
     ax = fma(-dx, fac, ax);
     ay = fma(-dy, fac, ay);
