@@ -328,6 +328,49 @@ __device__ __forceinline__ double starter_series(double T, double rinv, double a
     return fma(T, ff_to_f64(sum), T);
 }
 
+// One FP32 Newton step on Kepler's equation in universal variables from a
+// starting guess s (the learned starter's), with the Stumpff functions in
+// FP32: the series to x^5 for |x| < 1 (x = alpha s^2), else the circular or
+// hyperbolic closed forms.  The FP32 residual is good to ~2e-7 of dt, so the
+// step leaves s within ~2e-7 of the root when the guess was within a few
+// per cent: well inside the basin where the first FP64 pass's predicted
+// acceptance holds, which a guess 1e-3 off can miss.  A step that is not
+// finite or larger than a tenth of s (a guess too far off for one step to
+// be trusted) leaves s unchanged for the FP64 passes.  One FP64 addition.
+__device__ __forceinline__ double refine_guess_f32(double s, double dt, double r0, double u, double mu,
+                                                   double alpha)
+{
+    const float sf = f32_trunc(s), af = f32_trunc(alpha);
+    const float x = af * sf * sf;
+    float c2, c3;
+    if (fabsf(x) < 1.0f) {
+        c2 = fmaf(x, fmaf(x, fmaf(x, fmaf(x, fmaf(x, -1.0f / 479001600.0f, 1.0f / 3628800.0f),
+                                                -1.0f / 40320.0f), 1.0f / 720.0f), -1.0f / 24.0f), 0.5f);
+        c3 = fmaf(x, fmaf(x, fmaf(x, fmaf(x, fmaf(x, -1.0f / 6227020800.0f, 1.0f / 39916800.0f),
+                                                -1.0f / 362880.0f), 1.0f / 5040.0f), -1.0f / 120.0f),
+                  1.0f / 6.0f);
+    } else if (x > 0.0f) {
+        const float w = sqrtf(x);
+        float sw, cw;
+        sincosf(w, &sw, &cw);
+        c2 = (1.0f - cw) / x;
+        c3 = (w - sw) / (x * w);
+    } else {
+        const float w = sqrtf(-x);
+        const float e = expf(w), ei = 1.0f / e;
+        c2 = (1.0f - 0.5f * (e + ei)) / x;
+        c3 = (w - 0.5f * (e - ei)) / (x * w);
+    }
+    const float s2 = sf * sf;
+    const float g1 = sf * fmaf(-x, c3, 1.0f), g2 = s2 * c2, g3 = s2 * sf * c3, g0 = fmaf(-x, c2, 1.0f);
+    const float r0f = f32_trunc(r0), uf = f32_trunc(u), muf = f32_trunc(mu);
+    const float f = fmaf(r0f, g1, fmaf(uf, g2, fmaf(muf, g3, -f32_trunc(dt))));
+    const float fp = fmaf(r0f, g0, fmaf(uf, g1, muf * g2));
+    const float ds = -f / fp;
+    if (!(fabsf(ds) <= 0.1f * fabsf(sf))) return s;
+    return s + f64_of_f32(ds);
+}
+
 struct DriftResult {
     uint16_t flags;     // 0x08 unbound, 0x04 not converged
     uint16_t evals;     // Stumpff evaluations spent
@@ -565,6 +608,9 @@ __device__ __forceinline__ DriftResult kepler_drift(double& rx, double& ry, doub
         if (res.wide) s = starter_learned<NET_ROWS, NET_QU>(mlp, T, rinv, q.tau2, u, mu_r, alpha);
     }
     const bool net = s > 0;     // -1 outside the training box (NaN fails too)
+    if constexpr (LEARNED) {
+        if (net) s = refine_guess_f32(s, dt, r0, u, mu, alpha);
+    }
     if (!net) {
         if (series) s = starter_series(T, rinv, alpha, u, mu_r);
         else if (res.wide && alpha > 0) s = starter_fp32_kepler(dt, r0, mu, alpha, u);
