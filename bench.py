@@ -744,12 +744,50 @@ def run_close_eccentric(G, args, rank, barrier):
         barrier()
         legs[name] = timed_blocks(G, sim, 2)
         del sim
-    return {"workload": "close-eccentric: Sun + Neptune-mass planet at 30 au, %d particles a~U(2.5,6) au "
-                        "e~U(0.1,0.6) i~U(0,20deg), dt=180 d, Time-Block-Size 512" % len(r),
-            "training": {"samples": tr.samples()[0], "steps": args.close_train_steps, "batch": args.close_batch,
-                         "lr": 2e-2, "loss_last": float(losses[-100:].mean())},
-            "starters": legs, "learned_vs_classic": legs["learned"]["value"] / legs["classic"]["value"],
-            "learned_vs_series_presolve": legs["learned"]["value"] / legs["series"]["value"]}
+    out = {"workload": "close-eccentric: Sun + Neptune-mass planet at 30 au, %d particles a~U(2.5,6) au "
+                       "e~U(0.1,0.6) i~U(0,20deg), dt=180 d, Time-Block-Size 512" % len(r),
+           "training": {"samples": tr.samples()[0], "steps": args.close_train_steps, "batch": args.close_batch,
+                        "lr": 2e-2, "loss_last": float(losses[-100:].mean())},
+           "starters": legs, "learned_vs_classic": legs["learned"]["value"] / legs["classic"]["value"],
+           "learned_vs_series_presolve": legs["learned"]["value"] / legs["series"]["value"]}
+    if not args.no_close_ensembles:
+        out["ensembles"] = run_close_ensembles(G, args, rank, path, barrier)
+    return out
+
+
+def run_close_ensembles(G, args, rank, path, barrier, n_systems=64, T=512):
+    """Learned + batched where the network runs: 64 systems, each the Sun +
+    a Neptune-mass planet (mass x U(0.9, 1.1), a x U(0.95, 1.05)), with
+    close-eccentric particles (lognormal counts, median 2e4), in the batched
+    kernel with the series rule (its FP32 pre-solve on every drift here) and
+    with the learned starter (the close-eccentric leg's network)."""
+    from glisser_gb300 import synth
+    counts = synth.ensemble_counts(n_systems, seed=500 + rank)
+    sub = []
+    for s in range(n_systems):
+        rng = np.random.default_rng(500 + rank + s)
+        m, pel = synth.neptune_planets()
+        m = m.copy()
+        m[1] *= rng.uniform(0.9, 1.1)
+        pel = pel.copy()
+        pel[0, 0] *= rng.uniform(0.95, 1.05)
+        sub.append((m, pel, synth.particle_elements(rng, int(counts[s]), (2.5, 6.0), (0.1, 0.6), 20.0)))
+    systems = to_cartesian(G.elements_to_cartesian, sub)
+    out = {"workload": "%d systems (Sun + Neptune-mass planet, mass x U(0.9,1.1), a x U(0.95,1.05)), "
+                       "%d close-eccentric particles a~U(2.5,6) au e~U(0.1,0.6) i~U(0,20deg), dt=180 d, "
+                       "Time-Block-Size %d, 128 threads x 1" % (n_systems, int(counts.sum()), T)}
+    flags = {}
+    for name, st in (("batched_series", G.STARTER_SERIES), ("batched_learned", G.STARTER_LEARNED)):
+        ens = make_ensemble(G, systems, T, st, path if st == G.STARTER_LEARNED else None, (128, 1))
+        el, kms, d, _ = time_ensemble(ens, 2, 2, barrier)
+        out[name] = {"value": d["particle_steps"] / (el * 1e-3), "unit": UNIT,
+                     "kepler_evals_per_particle_step": d["kepler_evals"] / max(d["particle_steps"], 1),
+                     "network_blocks": d["network_blocks"], "network_drifts": d["learned_drifts"]}
+        flags[name] = ens.get_state()[2]
+        del ens
+    out["learned_vs_series"] = out["batched_learned"]["value"] / out["batched_series"]["value"]
+    out["flags_identical"] = bool(np.array_equal(flags["batched_series"], flags["batched_learned"]))
+    return out
 
 
 def run_history(G, args, rank, path, barrier):
@@ -900,6 +938,7 @@ def main():
     ap.add_argument("--close-batch", type=int, default=65536)
     ap.add_argument("--no-scattered", action="store_true")
     ap.add_argument("--no-close", action="store_true")
+    ap.add_argument("--no-close-ensembles", action="store_true")
     ap.add_argument("--no-history", action="store_true")
     ap.add_argument("--history-particles", type=int, default=2_000_000)
     ap.add_argument("--history-blocks", type=int, default=20)

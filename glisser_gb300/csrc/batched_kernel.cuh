@@ -15,13 +15,15 @@ using namespace tile;
 // pipe ~65 % busy, issue ~57 % at 5 CTAs of 128), so it is sized for 8 CTAs
 // of 128 per SM (64 registers, ~100 bytes of spills; 64-step planet-log
 // chunks fit 8 CTAs' shared memory): 6 % faster than 5 CTAs at 93
-// registers, and ahead of 6, 7 and 9 CTAs.  The learned-starter kernel keeps
-// 512 (its network's registers).
+// registers, and ahead of 6, 7 and 9 CTAs.  The learned-starter kernel is
+// sized the same: on ensembles whose every drift runs the network it
+// measured 1.6 % faster at 8 CTAs (64 registers, its network's activations
+// and spills in local memory) than at 4 (96 registers).
 #ifndef GLISSER_BATCHED_THREADS_PER_SM
 #define GLISSER_BATCHED_THREADS_PER_SM 1024
 #endif
 #ifndef GLISSER_BATCHED_THREADS_PER_SM_LEARNED
-#define GLISSER_BATCHED_THREADS_PER_SM_LEARNED 512
+#define GLISSER_BATCHED_THREADS_PER_SM_LEARNED GLISSER_BATCHED_THREADS_PER_SM
 #endif
 
 // Persistent kernel over (system, tile) work items.  The learned starter
