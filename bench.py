@@ -744,6 +744,50 @@ def run_close_eccentric(G, args, rank, barrier):
         barrier()
         legs[name] = timed_blocks(G, sim, 2)
         del sim
+    # a sample against the oracle's universal-variable drift (the reference's
+    # kepu spec) over two blocks, in its converged mode: at eight steps per
+    # orbit the reference's acceptance (G-functions at the point whose
+    # residual passed, up to 1e-13 of dt per drift) accumulates to ~1e-8 over
+    # 1024 steps, so the default mode's spread is reported beside it
+    from oracle import oracle as O
+    O.build()
+    ns = 4096
+    runs = {}
+    for key, conv, r_in in (("converged", True, r[:ns]), ("default", False, r[:ns]),
+                            ("ulp", True, np.nextafter(r[:ns], np.inf))):
+        O.set_kepu_converged(conv)
+        ex = O.Exec(m, pr, pv, np.arange(len(m)), r_in, v[:ns], np.arange(ns), dt=180.0, tbsize=512,
+                    outer_r=1e5, drift="uv")
+        for _ in range(2):
+            ex.loop()
+        p = ex.particles()
+        o = np.argsort(p["id"])
+        runs[key] = {k: p[k][o] for k in ("r", "flags")}
+        del ex
+    O.set_kepu_converged(False)
+    want = runs["converged"]
+
+    def spread(x):
+        return np.linalg.norm(x["r"] - want["r"], axis=1) / np.linalg.norm(want["r"], axis=1)
+    for name, st in (("classic", G.STARTER_CLASSIC), ("series", G.STARTER_SERIES), ("learned", G.STARTER_LEARNED)):
+        sim = G.Simulation(config_text(512, 180.0, outer=1e5))
+        sim.set_planets(m, pr, pv)
+        sim.set_particles(r[:ns], v[:ns])
+        sim.set_starter(st, path if st == G.STARTER_LEARNED else None)
+        sim.init()
+        for _ in range(2):
+            sim.loop()
+        got = sim.particles()
+        go = np.argsort(got["id"])
+        live = want["flags"] == 0
+        d = np.linalg.norm(got["r"][go] - want["r"], axis=1) / np.linalg.norm(want["r"], axis=1)
+        legs[name]["vs_oracle"] = {"particles": ns, "steps": 1024, "max_rel_pos_err": float(d[live].max()),
+                                   "q999": float(np.quantile(d[live], 0.999)),
+                                   "flags_identical": bool(np.array_equal(got["flags"][go], want["flags"])),
+                                   "oracle": "universal-variable drift, converged mode",
+                                   "oracle_default_mode_spread": float(spread(runs["default"])[live].max()),
+                                   "rounding_floor": float(spread(runs["ulp"])[live].max())}
+        del sim
     out = {"workload": "close-eccentric: Sun + Neptune-mass planet at 30 au, %d particles a~U(2.5,6) au "
                        "e~U(0.1,0.6) i~U(0,20deg), dt=180 d, Time-Block-Size 512" % len(r),
            "training": {"samples": tr.samples()[0], "steps": args.close_train_steps, "batch": args.close_batch,

@@ -224,6 +224,26 @@ static void kepu_stumpff(double x, double* c0, double* c1, double* c2, double* c
 	}
 }
 
+/* Checker option, off by default (then the reference's arithmetic): on
+ * acceptance, evaluate the G-functions at the s that the accepting pass
+ * corrected to, not at the s whose residual passed, so that each drift is
+ * converged to O(DANBYB^2) instead of carrying up to DANBYB of dt.  For
+ * comparisons on workloads with few steps per orbit, where the reference's
+ * per-drift residual accumulates above the parity tolerance. */
+static int g_kepu_converged = 0;
+void orc_set_kepu_converged(int on) { g_kepu_converged = on; }
+
+static void kepu_at(double s, double mu, double alpha, double r0, double u, double* fp, double* c1, double* c2,
+	double* c3)
+{
+	double c0;
+	kepu_stumpff(s * s * alpha, &c0, c1, c2, c3);
+	*c1 = *c1 * s;
+	*c2 = *c2 * s * s;
+	*c3 = *c3 * s * s * s;
+	*fp = r0 * c0 + u * *c1 + mu * *c2;
+}
+
 /* src/wh.cpp:260-290; *iters receives the number of passes */
 static int kepu_new(double s, double dt, double r0, double mu, double alpha, double u,
 	double* fp, double* c1, double* c2, double* c3, int* iters)
@@ -246,7 +266,11 @@ static int kepu_new(double s, double dt, double r0, double mu, double alpha, dou
 		s = s + ds;
 		double fdt = f / dt;
 		if (iters) *iters = nc + 1;
-		if (fdt * fdt < DANBYB * DANBYB) return 0;
+		if (fdt * fdt < DANBYB * DANBYB)
+		{
+			if (g_kepu_converged) kepu_at(s, mu, alpha, r0, u, fp, c1, c2, c3);
+			return 0;
+		}
 	}
 	return 1;
 }
@@ -283,7 +307,11 @@ static int kepu_lag(double s, double dt, double r0, double mu, double alpha, dou
 		double ds = -ln * f / (*fp + (*fp > 0 ? 1 : -1) * sqrt(fabs((ln - 1.) * (ln - 1.) * *fp * *fp - (ln - 1.) * ln * f * fpp)));
 		s = s + ds;
 		double fdt = f / dt;
-		if (fdt * fdt < DANBYB * DANBYB) return 0;
+		if (fdt * fdt < DANBYB * DANBYB)
+		{
+			if (g_kepu_converged) kepu_at(s, mu, alpha, r0, u, fp, c1, c2, c3);
+			return 0;
+		}
 	}
 	return 1;
 }

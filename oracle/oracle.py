@@ -50,6 +50,8 @@ def lib():
         L.orc_kepu.argtypes = [C.c_double] * 5 + [D, D, D, D, I32]
         L.orc_kepu.restype = C.c_int
         L.orc_kepu_guess.argtypes = [C.c_double] * 5 + [D]
+        L.orc_set_kepu_converged.argtypes = [C.c_int]
+        L.orc_set_kepu_converged.restype = None
         L.orc_uv_drift.argtypes = [C.c_size_t, D, D, U16, C.c_double, C.c_double, I32]
         L.orc_from_elements_M.argtypes = [C.c_double] * 7 + [D, D]
         L.orc_from_elements.argtypes = [C.c_double] * 7 + [D, D]
@@ -128,6 +130,14 @@ def block(r, v, a, flags, tbsize, npl, h0_log, r_log, m, pl_id, rh, outer_r, dt,
                     _p(np.ascontiguousarray(pl_id, np.uint32), U32), _p(np.ascontiguousarray(rh, np.float64), D),
                     outer_r, dt, mu)
     return flags, dti
+
+
+def set_kepu_converged(on):
+    """Checker option (off by default, then the reference's arithmetic): the
+    universal-variable drift takes its G-functions at the accepting pass's
+    corrected s, converged to O(1e-26) instead of carrying up to 1e-13 of dt
+    per drift."""
+    lib().orc_set_kepu_converged(1 if on else 0)
 
 
 def kepu(dt, r0, mu, alpha, u):
