@@ -130,3 +130,33 @@ def test_threebody_example_matches_reference():
     live = g["out49_flags"][np.argsort(g["out49_id"])] == 0
     assert np.allclose(maxerr[live], g["cj_maxerr"][live], rtol=1e-6, atol=1e-15)
     assert g["cj_maxerr"][live].max() < 1e-7
+
+
+def test_converged_kepu_option():
+    """The checker option for workloads with few steps per orbit: off, kepu
+    stays the reference's (the pinned grid above); on, the G-functions come
+    from the accepting pass's corrected s, so the Kepler residual they give is
+    far below the reference's acceptance threshold (|f| < 1e-13 dt), and off
+    again restores the reference's results bit for bit."""
+    g = np.load(os.path.join(GOLD, "kepu_grid.npz"))
+    rows = [tuple(map(float, (g["dt"][k], g["r0"][k], g["mu"][k], g["alpha"][k], g["u"][k])))
+            for k in range(0, len(g["dt"]), 7)]
+
+    def residual(dt, r0, mu, alpha, u, c1, c2, c3):
+        return abs(r0 * c1 + u * c2 + mu * c3 - dt) / dt
+
+    try:
+        O.set_kepu_converged(True)
+        conv = [O.kepu(*row) for row in rows]
+    finally:
+        O.set_kepu_converged(False)
+    ref = [O.kepu(*row) for row in rows]
+    ok = [k for k, (a, b) in enumerate(zip(conv, ref)) if a[0] == 0 and b[0] == 0]
+    assert len(ok) > 0.9 * len(rows)
+    r_conv = np.array([residual(*rows[k], *conv[k][2:5]) for k in ok])
+    r_ref = np.array([residual(*rows[k], *ref[k][2:5]) for k in ok])
+    assert r_ref.max() < 1e-13
+    assert np.median(r_conv) < 0.1 * np.median(r_ref) or np.median(r_ref) < 1e-15
+    assert r_conv.max() < 1e-14
+    again = [O.kepu(*row) for row in rows]
+    assert all(np.array_equal(np.array(a[:5]), np.array(b[:5])) for a, b in zip(again, ref))
